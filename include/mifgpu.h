@@ -1,0 +1,168 @@
+/*
+ * mifgpu — one GB300 (sm_103a) time step of the staggered-grid incompressible
+ * Navier-Stokes solver of FattiMei/mpi-incompressible-fluid, behind a C ABI.
+ *
+ * The library owns device memory; the caller owns host memory. Host arrays are
+ * in the reference's own layout: one StaggeredTensor per field, x fastest,
+ * index i + Ex*(j + Ey*k) (include/Tensor.h:137-140,237), with the reference's
+ * extents per staggering (src/StaggeredTensor.cpp:5-9, src/Constants.cpp:80-88).
+ * mifgpu_field_extent() reports them.
+ *
+ * Every entry point returns MIFGPU_OK (0) or a negative MIFGPU_E* code;
+ * mifgpu_last_error() gives the message. A context is bound to the CUDA device
+ * that was current at mifgpu_create() and to one stream; it is not thread-safe
+ * (the reference's solver state is not re-entrant either,
+ * src/PressureSolverStructures.cpp:13-70).
+ *
+ * Field ids (the reference's tensors passed to mif::timestep,
+ * include/Timestep.h:16-19):
+ *   0..2  velocity.{u,v,w}            3..5  velocity_buffer.{u,v,w}
+ *   6..8  velocity_buffer_2.{u,v,w}   9     pressure
+ *   10    pressure_buffer (the Poisson solution phi of the last solve)
+ */
+#ifndef MIFGPU_H
+#define MIFGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MIFGPU_OK 0
+#define MIFGPU_EINVAL (-1)   /* bad argument (null pointer, size, id, mode) */
+#define MIFGPU_ECUDA (-2)    /* a CUDA call failed; see mifgpu_last_error */
+#define MIFGPU_ENOMEM (-3)   /* device allocation failed */
+#define MIFGPU_ENOTSUP (-4)  /* combination the reference does not define */
+#define MIFGPU_ENONFINITE (-5) /* the step produced NaN/Inf (watchdog) */
+
+enum mifgpu_precision {
+  MIFGPU_FP64 = 0,  /* everything in double: the reference's USE_DOUBLE=1 build */
+  MIFGPU_MIXED = 1  /* fields and stencils in float; eigenvalue division,
+                       zero-mode handling and reductions in double */
+};
+
+/* Analytic field families used for Dirichlet boundary data, forcing and
+ * error norms (the reference passes them as std::function,
+ * include/VectorFunction.h:33-53). */
+enum mifgpu_field_kind {
+  MIFGPU_FIELD_ZERO = 0,   /* no-slip walls / periodic boxes */
+  MIFGPU_FIELD_SINCOS = 1, /* u = sin x cos y sin z sin t, v = cos x sin y sin z sin t,
+                              w = 2 cos x cos y cos z sin t, p = cos x cos y sin z sin t
+                              (generators/manufsol_velocity.py:55-57) */
+  MIFGPU_FIELD_ETHIER = 2  /* exact NS solution of test/full_test.cpp
+                              (generators/manufsol.py:35-72) */
+};
+
+/* Forcing added to the momentum right-hand side of the projection step.
+ * The reference's mif::timestep has none (src/Timestep.cpp:16,32,49); the
+ * two others are extensions for manufactured-solution runs. */
+enum mifgpu_forcing {
+  MIFGPU_FORCING_NONE = 0,
+  MIFGPU_FORCING_VELOCITY = 1,     /* u_t + (u.grad)u - lap(u)/Re of the SINCOS velocity,
+                                      include/MomentumEquationForcing.h:10-32 */
+  MIFGPU_FORCING_NAVIER_STOKES = 2 /* the same plus grad p of the SINCOS pressure */
+};
+
+typedef struct {
+  long n_global[3];  /* points per axis, include/Constants.h:14-16: a periodic axis
+                        with N unique points has N + 1; a Dirichlet axis counts
+                        both walls */
+  double size[3];    /* domain lengths (x_size, y_size_global, z_size_global) */
+  double origin[3];  /* min_x_global, min_y_global, min_z_global */
+  double Re;         /* Reynolds number */
+  double dt;         /* time step (Constants::dt) */
+  int periodic[3];   /* periodic_bc */
+  int precision;     /* enum mifgpu_precision */
+  int boundary_kind; /* enum mifgpu_field_kind: exact velocity on Dirichlet faces */
+  int forcing;       /* enum mifgpu_forcing */
+} mifgpu_params;
+
+typedef struct mifgpu_ctx mifgpu_ctx;
+
+/* Replaces the set-up of src/main.cpp:127-141: Constants,
+ * PressureSolverStructures (src/PressureSolverStructures.cpp:13-70) and the
+ * six tensors. All fields start at zero. */
+int mifgpu_create(const mifgpu_params *params, mifgpu_ctx **out);
+int mifgpu_destroy(mifgpu_ctx *ctx);
+
+/* Stream for every launch and copy (default: a stream the context creates).
+ * `stream` is a cudaStream_t. */
+int mifgpu_set_stream(mifgpu_ctx *ctx, void *stream);
+int mifgpu_synchronize(mifgpu_ctx *ctx);
+const char *mifgpu_last_error(const mifgpu_ctx *ctx);
+
+/* Extents (Ex, Ey, Ez) of a field in the reference layout. */
+int mifgpu_field_extent(const mifgpu_ctx *ctx, int field, long out[3]);
+
+/* Host <-> device copies of one field in the reference layout (double).
+ * upload is asynchronous on the context's stream: the host buffer must stay
+ * valid until the next synchronising call. download returns after the data
+ * has landed in `host`. */
+int mifgpu_upload(mifgpu_ctx *ctx, int field, const double *host);
+int mifgpu_download(mifgpu_ctx *ctx, int field, double *host);
+
+/* Initial conditions from the analytic family (test/full_test.cpp:86-89):
+ * velocity set `set` (0..2) sampled at time t on every point, or the pressure. */
+int mifgpu_set_exact_velocity(mifgpu_ctx *ctx, int set, double t);
+int mifgpu_set_exact_pressure(mifgpu_ctx *ctx, double t);
+
+/* One projection step from t_n, replaces mif::timestep
+ * (include/Timestep.h:16-19, src/Timestep.cpp:151-156). Works on the
+ * device-resident fields. */
+int mifgpu_timestep(mifgpu_ctx *ctx, double t_n);
+
+/* `nsteps` projection steps from t0 with t_n = t0 + n*dt, replayed from one
+ * captured CUDA graph (the loop of src/main.cpp:149-156). */
+int mifgpu_run(mifgpu_ctx *ctx, double t0, int nsteps);
+
+/* The drop-in form of mif::timestep for callers that keep the fields on the
+ * host: uploads velocity (u,v,w) and pressure, steps, downloads them back.
+ * Buffers are in the reference layout (extents of fields 0,1,2,9). */
+int mifgpu_timestep_host(mifgpu_ctx *ctx, double t_n, double *u, double *v, double *w, double *p);
+
+/* Non-homogeneous Neumann pressure variant, replaces mif::timestep_nhn
+ * (src/Timestep.cpp:143-149); the pressure-gradient data is the gradient of
+ * the boundary kind's pressure. Requires no periodic axis. */
+int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n);
+
+/* Velocity-only RK3 step with the SINCOS forcing, replaces
+ * mif::timestep_velocity (src/TimestepVelocity.cpp:60-90): uses sets 0..2 as
+ * velocity, velocity_buffer and rhs_buffer, and ends with the swap of
+ * src/TimestepVelocity.cpp:89. */
+int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n);
+
+/* Sub-steps, for parity testing and for callers that assemble their own step:
+ *   apply_bc       VelocityTensor::apply_bc on set `set` at time t
+ *                  (src/VelocityTensor.cpp:36-233)
+ *   solve_pressure solve_pressure_equation_homogeneous_periodic: phi from
+ *                  div(set)/dt (src/PressureEquation.cpp:266-274)
+ *   divergence     phi := div(set)/dt on owner points only
+ *                  (src/PressureEquation.cpp:59-61)
+ *   project        p += phi and set -= dt * grad(phi) on interior points
+ *                  (src/Timestep.cpp:66-81) */
+int mifgpu_apply_bc(mifgpu_ctx *ctx, int set, double t);
+int mifgpu_solve_pressure(mifgpu_ctx *ctx, int set, double dt);
+int mifgpu_divergence(mifgpu_ctx *ctx, int set, double dt);
+int mifgpu_project(mifgpu_ctx *ctx, int set, double dt);
+
+/* Mean shift of the pressure towards the boundary kind's exact pressure at t
+ * (adjust_pressure, src/PressureEquation.cpp:288-343), in double. */
+int mifgpu_adjust_pressure(mifgpu_ctx *ctx, double t);
+
+/* The nine numbers of test/full_test.cpp:150-175 against the boundary kind's
+ * exact fields at t: L1, L2, Linf of velocity, pressure, pressure gradient
+ * (src/Norms.cpp:11-118). Reductions in double. */
+int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]);
+
+/* Number of kernels this context has launched so far (for launch accounting). */
+int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out);
+
+/* Device bytes held by the context. */
+int mifgpu_device_bytes(const mifgpu_ctx *ctx, size_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MIFGPU_H */

@@ -1,0 +1,621 @@
+// C ABI of mifgpu (include/mifgpu.h): context set-up, host transfers, and the
+// orchestration of one projection step as a single captured CUDA graph.
+//
+// Step structure (src/Timestep.cpp:97-141), all on the context's stream:
+//   for each stage k: stage update -> boundary fill -> divergence ->
+//   Poisson solve (5 line sweeps) -> periodic refresh of phi -> projection
+// Stage times are read by the kernels from a device slot array, so one graph
+// replays every step of a run without re-capture.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mifgpu.h"
+#include "common.cuh"
+#include "poisson.cuh"
+#include "stencil.cuh"
+
+using namespace mifgpu;
+
+namespace {
+
+struct ImplBase {
+  virtual ~ImplBase() = default;
+  virtual int init(mifgpu_ctx *ctx) = 0;
+  virtual void *field_ptr(int id) = 0;
+  virtual int upload(mifgpu_ctx *ctx, int id, const double *host) = 0;
+  virtual int download(mifgpu_ctx *ctx, int id, double *host) = 0;
+  virtual int set_exact(mifgpu_ctx *ctx, int id, double t) = 0;
+  virtual int step(mifgpu_ctx *ctx, int variant, const double *slots, int nsteps) = 0;
+  virtual int apply_bc(mifgpu_ctx *ctx, int set, double t) = 0;
+  virtual int solve_pressure(mifgpu_ctx *ctx, int set, double dt, bool solve) = 0;
+  virtual int project(mifgpu_ctx *ctx, int set, double dt) = 0;
+  virtual int adjust_pressure(mifgpu_ctx *ctx, double t) = 0;
+  virtual int error_norms(mifgpu_ctx *ctx, double t, double out[9]) = 0;
+  virtual void swap_sets() = 0;
+  virtual size_t bytes() const = 0;
+};
+
+}  // namespace
+
+struct mifgpu_ctx {
+  mifgpu_params prm{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  Geometry g{};
+  std::string err;
+  long long launches = 0;
+  std::unique_ptr<ImplBase> impl;
+};
+
+namespace {
+
+int fail(mifgpu_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_fail(mifgpu_ctx *ctx, cudaError_t e, const char *where) {
+  return fail(ctx, MIFGPU_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+// Extents of field id in the reference layout.
+void field_extent(const Geometry &g, int id, int e[3]) {
+  if (id < 9) {
+    const int c = id % 3;
+    for (int d = 0; d < 3; ++d) e[d] = g.ext(c, d);
+  } else {
+    for (int d = 0; d < 3; ++d) e[d] = g.E[d];
+  }
+}
+
+// Times of one projection step, computed as src/Timestep.cpp:97-104 does.
+void projection_slot(double t_n, double dt, double *s) {
+  const double dt_1 = 64.0 / 120.0 * dt;
+  const double time_1 = t_n + dt_1;
+  const double dt_2 = 16.0 / 120.0 * dt;
+  const double time_2 = time_1 + dt_2;
+  const double final_time = t_n + dt;
+  s[0] = t_n;
+  s[1] = time_1;
+  s[2] = time_2;
+  s[3] = final_time;
+  s[4] = std::sin(t_n);
+  s[5] = std::cos(t_n);
+  s[6] = std::sin(time_1);
+  s[7] = std::cos(time_1);
+  s[8] = std::sin(time_2);
+  s[9] = std::cos(time_2);
+}
+
+// Times of one velocity-only step, src/TimestepVelocity.cpp:63-65.
+void velocity_slot(double t_n, double dt, double *s) {
+  const double c2 = (8.0 / 15.0), c3 = (2.0 / 3.0);
+  const double time_1 = t_n + c2 * dt;
+  const double time_2 = t_n + c3 * dt;
+  const double final_time = t_n + dt;
+  s[0] = t_n;
+  s[1] = time_1;
+  s[2] = time_2;
+  s[3] = final_time;
+  s[4] = std::sin(t_n);
+  s[5] = std::cos(t_n);
+  s[6] = std::sin(time_1);
+  s[7] = std::cos(time_1);
+  s[8] = std::sin(time_2);
+  s[9] = std::cos(time_2);
+}
+
+enum { kVariantProjection = 0, kVariantNhn = 1, kVariantVelocity = 2 };
+
+// Last node of every captured step: the next replay reads the next time slot.
+__global__ void advance_step_kernel(int *ctr) { *ctr += 1; }
+
+template <typename T>
+struct Impl final : ImplBase {
+  Geometry g{};
+  size_t field_elems = 0;
+  T *block = nullptr;
+  Fields<T> phys{};  // physical field pointers
+  int parity = 0;    // 1 after an odd number of velocity-only steps: sets 0 and 1 exchanged
+  Fields<T> F{};     // logical view (reference field ids) for the current parity
+  PoissonSolver<T> ps{};
+  T *ftab = nullptr;
+  int ftab_maxE = 0;
+  double *slots = nullptr;  // device: kSlotSize doubles per step
+  int slots_cap = 0;
+  int *step_ctr = nullptr;  // device step index the graph reads and advances
+  double *acc = nullptr;    // device reduction scratch
+  double *staging = nullptr;
+  size_t staging_elems = 0;
+  T *grad_block = nullptr;  // three fields for the pressure-gradient norm
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  long long graph_launches[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  size_t total_bytes = 0;
+
+  ~Impl() override {
+    for (auto &gv : graph)
+      for (auto &gx : gv)
+        if (gx) cudaGraphExecDestroy(gx);
+    ps.release();
+    cudaFree(block);
+    cudaFree(ftab);
+    cudaFree(slots);
+    cudaFree(step_ctr);
+    cudaFree(acc);
+    cudaFree(staging);
+    cudaFree(grad_block);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+  }
+
+  int init(mifgpu_ctx *ctx) override {
+    g = ctx->g;
+    field_elems = (size_t)g.PX * g.PY * g.PZ;
+    cudaError_t e = cudaMalloc(&block, sizeof(T) * field_elems * kNumFields);
+    if (e != cudaSuccess) return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the field block failed");
+    total_bytes += sizeof(T) * field_elems * kNumFields;
+    CK(cudaMemset(block, 0, sizeof(T) * field_elems * kNumFields));
+    for (int f = 0; f < kNumFields; ++f) phys.f[f] = block + f * field_elems;
+    remap();
+    std::string perr;
+    const int rc = ps.init(g, perr);
+    if (rc) return fail(ctx, rc == -2 ? MIFGPU_ECUDA : MIFGPU_ENOTSUP, perr);
+    // Forcing tables: sin/cos at nodes and faces of each axis (host libm, double).
+    ftab_maxE = std::max({g.Es[0], g.Es[1], g.Es[2]}) + 1;
+    std::vector<T> tab((size_t)3 * 2 * 2 * ftab_maxE);
+    for (int ax = 0; ax < 3; ++ax)
+      for (int face = 0; face < 2; ++face)
+        for (int i = 0; i < ftab_maxE; ++i) {
+          const double x = face ? g.face(ax, i) : g.node(ax, i);
+          tab[((ax * 2 + face) * 2 + 0) * ftab_maxE + i] = T(std::sin(x));
+          tab[((ax * 2 + face) * 2 + 1) * ftab_maxE + i] = T(std::cos(x));
+        }
+    CK(cudaMalloc(&ftab, sizeof(T) * tab.size()));
+    CK(cudaMemcpy(ftab, tab.data(), sizeof(T) * tab.size(), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&step_ctr, sizeof(int)));
+    CK(cudaMemset(step_ctr, 0, sizeof(int)));
+    CK(cudaMalloc(&acc, sizeof(double) * 16));
+    CK(alloc_slots());
+    CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    return MIFGPU_OK;
+  }
+
+  // The slot array is allocated once: captured graphs hold its address.
+  static constexpr int kMaxSlots = 1024;
+  cudaError_t alloc_slots() {
+    cudaError_t e = cudaMalloc(&slots, sizeof(double) * kSlotSize * kMaxSlots);
+    if (e == cudaSuccess) slots_cap = kMaxSlots;
+    return e;
+  }
+
+  TimeRef tref() const { return TimeRef{slots, step_ctr}; }
+
+  void remap() {
+    F = phys;
+    if (parity)
+      for (int c = 0; c < 3; ++c) std::swap(F.f[c], F.f[3 + c]);
+  }
+
+  // swap_data of velocity and velocity_buffer (src/VelocityTensor.cpp:13-26)
+  // as a relabelling: captured graphs exist for both labellings.
+  void swap_sets() override {
+    parity ^= 1;
+    remap();
+  }
+
+  void *field_ptr(int id) override { return F.f[id]; }
+
+  int ensure_staging(mifgpu_ctx *ctx) {
+    const size_t need = (size_t)g.Es[0] * g.Es[1] * g.Es[2];
+    if (staging_elems >= need) return MIFGPU_OK;
+    cudaFree(staging);
+    staging = nullptr;
+    if (cudaMalloc(&staging, sizeof(double) * need) != cudaSuccess)
+      return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the transfer staging buffer failed");
+    total_bytes += sizeof(double) * need;
+    staging_elems = need;
+    return MIFGPU_OK;
+  }
+
+  int upload(mifgpu_ctx *ctx, int id, const double *host) override {
+    int e[3];
+    field_extent(g, id, e);
+    if (int rc = ensure_staging(ctx)) return rc;
+    const size_t n = (size_t)e[0] * e[1] * e[2];
+    CK(cudaMemcpyAsync(staging, host, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    launch_scatter<T>(g, F.f[id], staging, e[0], e[1], e[2], ctx->stream, &ctx->launches);
+    CK(cudaGetLastError());
+    return MIFGPU_OK;
+  }
+
+  int download(mifgpu_ctx *ctx, int id, double *host) override {
+    int e[3];
+    field_extent(g, id, e);
+    if (int rc = ensure_staging(ctx)) return rc;
+    const size_t n = (size_t)e[0] * e[1] * e[2];
+    launch_gather<T>(g, staging, F.f[id], e[0], e[1], e[2], ctx->stream, &ctx->launches);
+    CK(cudaMemcpyAsync(host, staging, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MIFGPU_OK;
+  }
+
+  int set_exact(mifgpu_ctx *ctx, int id, double t) override {
+    const int comp = id < 9 ? id % 3 : 3;
+    launch_set_exact<T>(g, F.f[id], comp, ctx->prm.boundary_kind, t, ctx->stream, &ctx->launches);
+    CK(cudaGetLastError());
+    return MIFGPU_OK;
+  }
+
+  // phi := div(set)/dt (+ Neumann flux) [-> Poisson solve -> periodic refresh]
+  void enqueue_pressure(mifgpu_ctx *ctx, cudaStream_t s, int set, double dt, bool nhn, int slot_new, int slot_old,
+                        bool solve, long long *cnt) {
+    T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
+    if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
+    if (!solve) return;
+    ps.solve(F.f[kPhi], s, cnt);
+    launch_periodic_scalar<T>(g, F.f[kPhi], s, cnt);
+  }
+
+  void enqueue_bc(mifgpu_ctx *ctx, cudaStream_t s, int set, int t_slot, long long *cnt) {
+    T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    launch_apply_bc<T>(g, vel, ctx->prm.boundary_kind, 0, tref(), t_slot, s, cnt);
+  }
+
+  void enqueue_project(cudaStream_t s, int set, double dt, long long *cnt) {
+    T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    launch_project<T>(g, F.f[kP], F.f[kPhi], vel, dt, s, cnt);
+  }
+
+  // The kernels of one step of the given variant, in stream order.
+  void enqueue_step(mifgpu_ctx *ctx, cudaStream_t s, int variant, long long *cnt) {
+    const double dt = g.dt;
+    ForcingTables<T> ft{ftab, ftab_maxE};
+    const int kind = ctx->prm.boundary_kind;
+    if (variant == kVariantVelocity) {
+      StageScalars<T> sc{dt, 4, 1};
+      launch_stage<T>(g, F, kVelY2, sc, ft, kind, tref(), s, cnt);
+      enqueue_bc(ctx, s, 1, 1, cnt);
+      sc.sin_slot = 6;
+      launch_stage<T>(g, F, kVelY3, sc, ft, kind, tref(), s, cnt);
+      enqueue_bc(ctx, s, 0, 2, cnt);
+      sc.sin_slot = 8;
+      launch_stage<T>(g, F, kVelUStar, sc, ft, kind, tref(), s, cnt);
+      enqueue_bc(ctx, s, 1, 3, cnt);
+      return;  // the final swap of sets 0 and 1 is done on the host side
+    }
+    const bool nhn = variant == kVariantNhn;
+    const double dts[3] = {64.0 / 120.0 * dt, 16.0 / 120.0 * dt, 40.0 / 120.0 * dt};
+    const StageKind kinds[3] = {kStageY2, kStageY3, kStageUStar};
+    const int out_set[3] = {1, 2, 0};
+    const int sin_slot[3] = {4, 6, 8};
+    for (int st = 0; st < 3; ++st) {
+      StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing};
+      launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt);
+      enqueue_bc(ctx, s, out_set[st], 1 + st, cnt);
+      enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt);
+      enqueue_project(s, out_set[st], dts[st], cnt);
+    }
+  }
+
+  int ensure_graph(mifgpu_ctx *ctx, int variant) {
+    if (graph[variant][parity]) return MIFGPU_OK;
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+    long long cnt = 0;
+    enqueue_step(ctx, cap_stream, variant, &cnt);
+    advance_step_kernel<<<1, 1, 0, cap_stream>>>(step_ctr);
+    ++cnt;
+    cudaError_t e = cudaStreamEndCapture(cap_stream, &gr);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream capture of the step");
+    e = cudaGraphInstantiate(&graph[variant][parity], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    graph_launches[variant][parity] = cnt;
+    return MIFGPU_OK;
+  }
+
+  int step(mifgpu_ctx *ctx, int variant, const double *host_slots, int nsteps) override {
+    if (int rc = ensure_graph(ctx, variant)) return rc;
+    for (int n0 = 0; n0 < nsteps; n0 += slots_cap) {
+      const int chunk = std::min(slots_cap, nsteps - n0);
+      CK(cudaMemcpyAsync(slots, host_slots + (size_t)kSlotSize * n0, sizeof(double) * kSlotSize * chunk,
+                         cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaMemsetAsync(step_ctr, 0, sizeof(int), ctx->stream));
+      for (int n = 0; n < chunk; ++n) {
+        CK(cudaGraphLaunch(graph[variant][parity], ctx->stream));
+        ctx->launches += graph_launches[variant][parity];
+      }
+    }
+    // The host copy of the slots may be a temporary: wait until it was consumed.
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MIFGPU_OK;
+  }
+
+  int write_single_slot(mifgpu_ctx *ctx, double t) {
+    double s[kSlotSize];
+    projection_slot(t, g.dt, s);
+    s[1] = s[2] = s[3] = t;  // sub-step calls use their own time in every slot
+    CK(cudaMemcpyAsync(slots, s, sizeof(s), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(step_ctr, 0, sizeof(int), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MIFGPU_OK;
+  }
+
+  int apply_bc(mifgpu_ctx *ctx, int set, double t) override {
+    if (int rc = write_single_slot(ctx, t)) return rc;
+    enqueue_bc(ctx, ctx->stream, set, 0, &ctx->launches);
+    CK(cudaGetLastError());
+    return MIFGPU_OK;
+  }
+
+  int solve_pressure(mifgpu_ctx *ctx, int set, double dt, bool solve) override {
+    enqueue_pressure(ctx, ctx->stream, set, dt, false, 0, 0, solve, &ctx->launches);
+    CK(cudaGetLastError());
+    return MIFGPU_OK;
+  }
+
+  int project(mifgpu_ctx *ctx, int set, double dt) override {
+    enqueue_project(ctx->stream, set, dt, &ctx->launches);
+    CK(cudaGetLastError());
+    return MIFGPU_OK;
+  }
+
+  int adjust_pressure(mifgpu_ctx *ctx, double t) override {
+    CK(cudaMemsetAsync(acc, 0, sizeof(double) * 4, ctx->stream));
+    launch_pressure_mean_diff<T>(g, F.f[kP], ctx->prm.boundary_kind, t, acc, ctx->stream, &ctx->launches);
+    launch_add_scalar<T>(g, F.f[kP], acc, ctx->stream, &ctx->launches);
+    CK(cudaGetLastError());
+    return MIFGPU_OK;
+  }
+
+  int error_norms(mifgpu_ctx *ctx, double t, double out[9]) override {
+    const int kind = ctx->prm.boundary_kind;
+    if (!grad_block) {
+      if (cudaMalloc(&grad_block, sizeof(T) * field_elems * 3) != cudaSuccess)
+        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the gradient scratch failed");
+      total_bytes += sizeof(T) * field_elems * 3;
+      CK(cudaMemset(grad_block, 0, sizeof(T) * field_elems * 3));
+    }
+    T *gv[3] = {grad_block, grad_block + field_elems, grad_block + 2 * field_elems};
+    T *vel[3] = {F.vel(0, 0), F.vel(0, 1), F.vel(0, 2)};
+    CK(cudaMemsetAsync(acc, 0, sizeof(double) * 9, ctx->stream));
+    launch_velocity_errors<T>(g, vel, kind, 0, t, acc, ctx->stream, &ctx->launches);
+    launch_pressure_errors<T>(g, F.f[kP], kind, t, acc + 3, ctx->stream, &ctx->launches);
+    launch_pressure_gradient<T>(g, gv, F.f[kP], ctx->stream, &ctx->launches);
+    if (int rc = write_single_slot(ctx, t)) return rc;
+    launch_apply_bc<T>(g, gv, kind, 1, tref(), 0, ctx->stream, &ctx->launches);
+    launch_velocity_errors<T>(g, gv, kind, 1, t, acc + 6, ctx->stream, &ctx->launches);
+    double h[9];
+    CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const double vol = g.h[0] * g.h[1] * g.h[2];
+    for (int b = 0; b < 3; ++b) {
+      const double *a = h + 3 * b;
+      if (b == 1) {
+        out[3 * b + 0] = a[0] * vol;  // sum |e| (scalar field)
+      } else {
+        out[3 * b + 0] = a[0] * vol;  // sum |e| (vector norm)
+      }
+      out[3 * b + 1] = std::sqrt(a[1] * vol);
+      out[3 * b + 2] = a[2];
+    }
+    return MIFGPU_OK;
+  }
+
+  size_t bytes() const override { return total_bytes; }
+};
+
+bool valid_field(int id) { return id >= 0 && id < kNumFields; }
+
+}  // namespace
+
+extern "C" {
+
+int mifgpu_create(const mifgpu_params *p, mifgpu_ctx **out) {
+  if (!p || !out) return MIFGPU_EINVAL;
+  *out = nullptr;
+  auto ctx = std::make_unique<mifgpu_ctx>();
+  ctx->prm = *p;
+  if (p->precision != MIFGPU_FP64 && p->precision != MIFGPU_MIXED)
+    return MIFGPU_EINVAL;
+  if (p->boundary_kind < 0 || p->boundary_kind > 2 || p->forcing < 0 || p->forcing > 2) return MIFGPU_EINVAL;
+  if (!(p->Re > 0) || !(p->dt > 0)) return MIFGPU_EINVAL;
+  Geometry &g = ctx->g;
+  for (int d = 0; d < 3; ++d) {
+    const int per = p->periodic[d] != 0;
+    if (p->n_global[d] < 3 || p->n_global[d] > (1 << 20) || !(p->size[d] > 0)) return MIFGPU_EINVAL;
+    g.n_global[d] = (int)p->n_global[d];
+    g.periodic[d] = per;
+    g.h[d] = p->size[d] / (double)(p->n_global[d] - 1);
+    g.oh[d] = 1 / g.h[d];
+    g.o2h[d] = 1 / (2 * g.h[d]);
+    g.o8h[d] = 1 / (8 * g.h[d]);
+    g.oh2Re[d] = 1 / (p->Re * g.h[d] * g.h[d]);
+    g.h_2[d] = g.h[d] / 2;
+    g.origin[d] = p->origin[d];
+    g.E[d] = per ? g.n_global[d] + 1 : g.n_global[d];
+    g.base[d] = per ? -1 : 0;
+    g.np[d] = g.n_global[d] - per;
+    g.own_lo[d] = per;
+  }
+  // One rank: the y and z staggered extents always gain a point, x only on a
+  // Dirichlet axis (src/Constants.cpp:86-88).
+  g.Es[0] = g.periodic[0] ? g.E[0] : g.E[0] + 1;
+  g.Es[1] = g.E[1] + 1;
+  g.Es[2] = g.E[2] + 1;
+  g.PX = ((long)std::max(g.Es[0], g.E[0]) + 7) / 8 * 8;
+  g.PY = g.Es[1];
+  g.PZ = g.Es[2];
+  g.Re = p->Re;
+  g.dt = p->dt;
+  if (cudaGetDevice(&ctx->device) != cudaSuccess) return fail(nullptr, MIFGPU_ECUDA, "no CUDA device");
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) return MIFGPU_ECUDA;
+  ctx->stream = ctx->own_stream;
+  if (p->precision == MIFGPU_FP64)
+    ctx->impl = std::make_unique<Impl<double>>();
+  else
+    ctx->impl = std::make_unique<Impl<float>>();
+  const int rc = ctx->impl->init(ctx.get());
+  if (rc != MIFGPU_OK) {
+    // keep the context so the caller can read the message
+    *out = ctx.release();
+    return rc;
+  }
+  *out = ctx.release();
+  return MIFGPU_OK;
+}
+
+int mifgpu_destroy(mifgpu_ctx *ctx) {
+  if (!ctx) return MIFGPU_EINVAL;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->impl.reset();
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return MIFGPU_OK;
+}
+
+int mifgpu_set_stream(mifgpu_ctx *ctx, void *stream) {
+  if (!ctx) return MIFGPU_EINVAL;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return MIFGPU_OK;
+}
+
+int mifgpu_synchronize(mifgpu_ctx *ctx) {
+  if (!ctx) return MIFGPU_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaGetLastError());
+  return MIFGPU_OK;
+}
+
+const char *mifgpu_last_error(const mifgpu_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int mifgpu_field_extent(const mifgpu_ctx *ctx, int field, long out[3]) {
+  if (!ctx || !out || !valid_field(field)) return MIFGPU_EINVAL;
+  int e[3];
+  field_extent(ctx->g, field, e);
+  for (int d = 0; d < 3; ++d) out[d] = e[d];
+  return MIFGPU_OK;
+}
+
+int mifgpu_upload(mifgpu_ctx *ctx, int field, const double *host) {
+  if (!ctx || !host || !valid_field(field)) return MIFGPU_EINVAL;
+  return ctx->impl->upload(ctx, field, host);
+}
+
+int mifgpu_download(mifgpu_ctx *ctx, int field, double *host) {
+  if (!ctx || !host || !valid_field(field)) return MIFGPU_EINVAL;
+  return ctx->impl->download(ctx, field, host);
+}
+
+int mifgpu_set_exact_velocity(mifgpu_ctx *ctx, int set, double t) {
+  if (!ctx || set < 0 || set > 2) return MIFGPU_EINVAL;
+  for (int c = 0; c < 3; ++c)
+    if (int rc = ctx->impl->set_exact(ctx, set * 3 + c, t)) return rc;
+  return MIFGPU_OK;
+}
+
+int mifgpu_set_exact_pressure(mifgpu_ctx *ctx, double t) {
+  if (!ctx) return MIFGPU_EINVAL;
+  return ctx->impl->set_exact(ctx, kP, t);
+}
+
+int mifgpu_timestep(mifgpu_ctx *ctx, double t_n) {
+  if (!ctx) return MIFGPU_EINVAL;
+  double s[kSlotSize];
+  projection_slot(t_n, ctx->g.dt, s);
+  return ctx->impl->step(ctx, kVariantProjection, s, 1);
+}
+
+int mifgpu_run(mifgpu_ctx *ctx, double t0, int nsteps) {
+  if (!ctx || nsteps < 0) return MIFGPU_EINVAL;
+  if (nsteps == 0) return MIFGPU_OK;
+  std::vector<double> s((size_t)kSlotSize * nsteps);
+  for (int n = 0; n < nsteps; ++n) projection_slot(t0 + n * ctx->g.dt, ctx->g.dt, s.data() + (size_t)kSlotSize * n);
+  return ctx->impl->step(ctx, kVariantProjection, s.data(), nsteps);
+}
+
+int mifgpu_timestep_host(mifgpu_ctx *ctx, double t_n, double *u, double *v, double *w, double *p) {
+  if (!ctx || !u || !v || !w || !p) return MIFGPU_EINVAL;
+  double *h[4] = {u, v, w, p};
+  const int ids[4] = {0, 1, 2, kP};
+  for (int q = 0; q < 4; ++q)
+    if (int rc = ctx->impl->upload(ctx, ids[q], h[q])) return rc;
+  if (int rc = mifgpu_timestep(ctx, t_n)) return rc;
+  for (int q = 0; q < 4; ++q)
+    if (int rc = ctx->impl->download(ctx, ids[q], h[q])) return rc;
+  return MIFGPU_OK;
+}
+
+int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n) {
+  if (!ctx) return MIFGPU_EINVAL;
+  if (ctx->g.periodic[0] || ctx->g.periodic[1] || ctx->g.periodic[2])
+    return fail(ctx, MIFGPU_ENOTSUP, "non-homogeneous Neumann data needs every axis non-periodic");
+  double s[kSlotSize];
+  projection_slot(t_n, ctx->g.dt, s);
+  return ctx->impl->step(ctx, kVariantNhn, s, 1);
+}
+
+int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n) {
+  if (!ctx) return MIFGPU_EINVAL;
+  double s[kSlotSize];
+  velocity_slot(t_n, ctx->g.dt, s);
+  if (int rc = ctx->impl->step(ctx, kVariantVelocity, s, 1)) return rc;
+  ctx->impl->swap_sets();  // src/TimestepVelocity.cpp:89
+  return MIFGPU_OK;
+}
+
+int mifgpu_apply_bc(mifgpu_ctx *ctx, int set, double t) {
+  if (!ctx || set < 0 || set > 2) return MIFGPU_EINVAL;
+  return ctx->impl->apply_bc(ctx, set, t);
+}
+
+int mifgpu_solve_pressure(mifgpu_ctx *ctx, int set, double dt) {
+  if (!ctx || set < 0 || set > 2 || !(dt != 0)) return MIFGPU_EINVAL;
+  return ctx->impl->solve_pressure(ctx, set, dt, true);
+}
+
+int mifgpu_divergence(mifgpu_ctx *ctx, int set, double dt) {
+  if (!ctx || set < 0 || set > 2 || !(dt != 0)) return MIFGPU_EINVAL;
+  return ctx->impl->solve_pressure(ctx, set, dt, false);
+}
+
+int mifgpu_project(mifgpu_ctx *ctx, int set, double dt) {
+  if (!ctx || set < 0 || set > 2) return MIFGPU_EINVAL;
+  return ctx->impl->project(ctx, set, dt);
+}
+
+int mifgpu_adjust_pressure(mifgpu_ctx *ctx, double t) {
+  if (!ctx) return MIFGPU_EINVAL;
+  return ctx->impl->adjust_pressure(ctx, t);
+}
+
+int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]) {
+  if (!ctx || !out) return MIFGPU_EINVAL;
+  return ctx->impl->error_norms(ctx, t, out);
+}
+
+int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out) {
+  if (!ctx || !out) return MIFGPU_EINVAL;
+  *out = ctx->launches;
+  return MIFGPU_OK;
+}
+
+int mifgpu_device_bytes(const mifgpu_ctx *ctx, size_t *out) {
+  if (!ctx || !out) return MIFGPU_EINVAL;
+  *out = ctx->impl->bytes();
+  return MIFGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,39 @@
+// Host interface of the spectral Poisson solver (poisson.cu).
+#pragma once
+
+#include <string>
+
+#include "common.cuh"
+
+namespace mifgpu {
+
+// Plan of the 1-D transform along one axis: kind, FFT factorisation, line
+// pairs per CTA, and device tables (twiddles in T, eigenvalues in double).
+template <typename T>
+struct AxisPlan {
+  int kind = 0;  // 0 DCT-I (Neumann), 1 real DFT (periodic)
+  int n = 0, L = 0;
+  int nfac = 0;
+  int fac[16] = {0};
+  int P = 1;
+  bool line_fast = false;
+  size_t smem = 0;
+  typename Vec2<T>::type *tw = nullptr;
+  double *lam_dev = nullptr;
+
+  int build(int kind, int n, double h, int line_count, bool line_fast, std::string &err);
+  void release();
+};
+
+template <typename T>
+struct PoissonSolver {
+  Geometry geo{};
+  AxisPlan<T> axis[3];
+
+  int init(const Geometry &g, std::string &err);
+  void release();
+  // In place on the owner block of phi: rhs in, solution out (no periodic refresh).
+  int solve(T *phi, cudaStream_t stream, long long *launches);
+};
+
+}  // namespace mifgpu

@@ -1,0 +1,117 @@
+// Host launchers of the point-wise kernels (stencil.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace mifgpu {
+
+// Device pointers of the eleven fields of a context, in the working precision.
+template <typename T>
+struct Fields {
+  T *f[kNumFields];
+  __host__ __device__ T *vel(int set, int c) const { return f[set * kFieldsPerSet + c]; }
+};
+
+enum StageKind {
+  kStageY2 = 0,     // src/Timestep.cpp:10-21
+  kStageY3 = 1,     // src/Timestep.cpp:24-39
+  kStageUStar = 2,  // src/Timestep.cpp:42-54
+  kVelY2 = 3,       // src/TimestepVelocity.cpp:20-29
+  kVelY3 = 4,       // src/TimestepVelocity.cpp:32-42
+  kVelUStar = 5     // src/TimestepVelocity.cpp:45-52
+};
+
+// Forcing tables: sin and cos of every node and face coordinate per axis,
+// evaluated on the host (libm, double) and stored in T.
+template <typename T>
+struct ForcingTables {
+  const T *tab = nullptr;  // [axis][0 node / 1 face][0 sin / 1 cos][maxE]
+  int maxE = 0;
+};
+
+// Stage times live in device memory so that a captured CUDA graph can be
+// replayed step after step: slot s of step n is slots[n * kSlotSize + s] with
+// n = *step. Layout of one step's slot (doubles):
+//   0 t_n, 1 time_1, 2 time_2, 3 final time,
+//   4/5 sin/cos(t_n), 6/7 sin/cos(time_1), 8/9 sin/cos(time_2)
+constexpr int kSlotSize = 10;
+struct TimeRef {
+  const double *slots;
+  const int *step;
+  __device__ __forceinline__ double get(int s) const { return slots[(long)(*step) * kSlotSize + s]; }
+};
+
+template <typename T>
+struct StageScalars {
+  double dt;     // Constants::dt
+  int sin_slot;  // slot of sin(stage time); cos follows it
+  int forcing;   // 0 none, 1 velocity forcing, 2 with grad p
+};
+
+template <typename T>
+void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
+                  const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches);
+
+// Dirichlet faces (fn 0 velocity family, 1 pressure-gradient family) then the
+// periodic copies, on velocity set `set` (src/VelocityTensor.cpp:36-233).
+template <typename T>
+void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn, TimeRef tr, int t_slot,
+                     cudaStream_t s, long long *launches);
+
+// Periodic ghost copy of a pressure-shaped field (src/StaggeredTensor.cpp:221-257).
+template <typename T>
+void launch_periodic_scalar(const Geometry &g, T *f, cudaStream_t s, long long *launches);
+
+// phi := div(vel)/dt on owner points (src/PressureEquation.cpp:59-61).
+template <typename T>
+void launch_divergence(const Geometry &g, T *phi, T *const vel[3], double dt, cudaStream_t s, long long *launches);
+
+// phi += boundary flux terms of the non-homogeneous Neumann problem
+// (src/PressureEquation.cpp:10-56), data = grad p(t_old) - grad p(t_new).
+template <typename T>
+void launch_neumann_flux(const Geometry &g, T *phi, int field_kind, TimeRef tr, int slot_new, int slot_old,
+                         cudaStream_t s, long long *launches);
+
+// p += phi everywhere; vel -= dt * grad(phi) on interior points (src/Timestep.cpp:66-81).
+template <typename T>
+void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, cudaStream_t s,
+                    long long *launches);
+
+// Reference layout (double, contiguous) <-> device layout (T, padded).
+template <typename T>
+void launch_scatter(const Geometry &g, T *dst, const double *src, int ex, int ey, int ez, cudaStream_t s,
+                    long long *launches);
+template <typename T>
+void launch_gather(const Geometry &g, double *dst, const T *src, int ex, int ey, int ez, cudaStream_t s,
+                   long long *launches);
+
+// Analytic initial fields (every point): comp 0..2 velocity component of a
+// set, 3 pressure.
+template <typename T>
+void launch_set_exact(const Geometry &g, T *f, int comp, int field_kind, double t, cudaStream_t s,
+                      long long *launches);
+
+// Sum of (exact p - p) over owner points into *acc (double, device).
+template <typename T>
+void launch_pressure_mean_diff(const Geometry &g, const T *p, int field_kind, double t, double *acc,
+                               cudaStream_t s, long long *launches);
+// p += *shift on every point.
+template <typename T>
+void launch_add_scalar(const Geometry &g, T *p, const double *shift, cudaStream_t s, long long *launches);
+
+// Error accumulators in double: acc[0] sum |e|-norm, acc[1] sum e^2, acc[2] max.
+template <typename T>
+void launch_velocity_errors(const Geometry &g, T *const vel[3], int field_kind, int fn, double t, double *acc,
+                            cudaStream_t s, long long *launches);
+template <typename T>
+void launch_pressure_errors(const Geometry &g, const T *p, int field_kind, double t, double *acc, cudaStream_t s,
+                            long long *launches);
+// gradient of p into the interior of vel (src/PressureGradient.h:9-24)
+template <typename T>
+void launch_pressure_gradient(const Geometry &g, T *const vel[3], const T *p, cudaStream_t s, long long *launches);
+
+// Non-finite watchdog: sets *flag if any of the n values is NaN/Inf.
+template <typename T>
+void launch_nonfinite_check(const T *f, long n, int *flag, cudaStream_t s, long long *launches);
+
+}  // namespace mifgpu

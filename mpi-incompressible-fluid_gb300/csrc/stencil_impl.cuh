@@ -1,0 +1,709 @@
+// Point-wise kernels of the time step (sm_103a): the three RK stage updates
+// with the fused momentum right-hand side, the boundary fill, the divergence,
+// the projection, layout conversion and the double-precision reductions.
+//
+// All three velocity components of a stage are computed by one thread per
+// point, so each launch streams the stage's inputs once. Expressions keep the
+// reference's evaluation order (include/MomentumEquation.h:42-255,
+// src/Timestep.cpp:10-54) so FP64 results stay within rounding of the CPU
+// solver.
+#pragma once
+
+#include <cmath>
+
+#include "analytic.cuh"
+#include "stencil.cuh"
+
+namespace mifgpu {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T ld(const T *p, long q) {
+  return __ldg(p + q);
+}
+
+// include/MomentumEquation.h:42-116 (OPT_CPU_CACHE branch)
+template <typename T>
+__device__ __forceinline__ T rhs_u(const T *u, const T *v, const T *w, long q, long sy, long sz, const Coeffs<T> &c) {
+  const T u13 = ld(u, q - 1), u11 = ld(u, q - sy), u5 = ld(u, q - sz), u14 = ld(u, q), u23 = ld(u, q + sz),
+          u17 = ld(u, q + sy), u15 = ld(u, q + 1);
+  const T v13 = ld(v, q - 1), v16 = ld(v, q - 1 + sy), v14 = ld(v, q), v17 = ld(v, q + sy);
+  const T w13 = ld(w, q - 1), w22 = ld(w, q - 1 + sz), w14 = ld(w, q), w23 = ld(w, q + sz);
+  const T conv = -u14 * (u15 - u13) * c.o2h[0] - (v17 + v14 + v16 + v13) * (u17 - u11) * c.o8h[1] -
+                 (w23 + w14 + w22 + w13) * (u23 - u5) * c.o8h[2];
+  const T diff = (u15 - T(2) * u14 + u13) * c.oh2Re[0] + (u17 - T(2) * u14 + u11) * c.oh2Re[1] +
+                 (u23 - T(2) * u14 + u5) * c.oh2Re[2];
+  return conv + diff;
+}
+
+// include/MomentumEquation.h:119-185
+template <typename T>
+__device__ __forceinline__ T rhs_v(const T *u, const T *v, const T *w, long q, long sy, long sz, const Coeffs<T> &c) {
+  const T u11 = ld(u, q - sy), u14 = ld(u, q), u12 = ld(u, q + 1 - sy), u15 = ld(u, q + 1);
+  const T v13 = ld(v, q - 1), v11 = ld(v, q - sy), v5 = ld(v, q - sz), v14 = ld(v, q), v23 = ld(v, q + sz),
+          v17 = ld(v, q + sy), v15 = ld(v, q + 1);
+  const T w11 = ld(w, q - sy), w20 = ld(w, q - sy + sz), w14 = ld(w, q), w23 = ld(w, q + sz);
+  const T conv = -(u15 + u14 + u12 + u11) * (v15 - v13) * c.o8h[0] - v14 * (v17 - v11) * c.o2h[1] -
+                 (w23 + w14 + w20 + w11) * (v23 - v5) * c.o8h[2];
+  const T diff = (v15 - T(2) * v14 + v13) * c.oh2Re[0] + (v17 - T(2) * v14 + v11) * c.oh2Re[1] +
+                 (v23 - T(2) * v14 + v5) * c.oh2Re[2];
+  return conv + diff;
+}
+
+// include/MomentumEquation.h:188-255
+template <typename T>
+__device__ __forceinline__ T rhs_w(const T *u, const T *v, const T *w, long q, long sy, long sz, const Coeffs<T> &c) {
+  const T u5 = ld(u, q - sz), u14 = ld(u, q), u6 = ld(u, q + 1 - sz), u15 = ld(u, q + 1);
+  const T v5 = ld(v, q - sz), v14 = ld(v, q), v8 = ld(v, q + sy - sz), v17 = ld(v, q + sy);
+  const T w13 = ld(w, q - 1), w11 = ld(w, q - sy), w5 = ld(w, q - sz), w14 = ld(w, q), w23 = ld(w, q + sz),
+          w17 = ld(w, q + sy), w15 = ld(w, q + 1);
+  const T conv = -(u15 + u14 + u6 + u5) * (w15 - w13) * c.o8h[0] - (v17 + v14 + v8 + v5) * (w17 - w11) * c.o8h[1] -
+                 w14 * (w23 - w5) * c.o2h[2];
+  const T diff = (w15 - T(2) * w14 + w13) * c.oh2Re[0] + (w17 - T(2) * w14 + w11) * c.oh2Re[1] +
+                 (w23 - T(2) * w14 + w5) * c.oh2Re[2];
+  return conv + diff;
+}
+
+// Momentum forcing of the SINCOS family at component c's staggered point,
+// from per-axis sin/cos tables: f = u_t + (u.grad)u - lap(u)/Re
+// (+ grad p), the residual generators/manufsol_velocity.py:32-50 derives.
+template <typename T>
+struct ForcingEval {
+  const T *tab;
+  int maxE;
+  T st, ct, invRe;
+  int with_p;
+  __device__ __forceinline__ T S(int ax, int face, int i) const { return tab[((ax * 2 + face) * 2 + 0) * maxE + i]; }
+  __device__ __forceinline__ T C(int ax, int face, int i) const { return tab[((ax * 2 + face) * 2 + 1) * maxE + i]; }
+  __device__ __forceinline__ T operator()(int c, int i, int j, int k) const {
+    const T sx = S(0, c == 0, i), cx = C(0, c == 0, i);
+    const T sy = S(1, c == 1, j), cy = C(1, c == 1, j);
+    const T sz = S(2, c == 2, k), cz = C(2, c == 2, k);
+    T f;
+    if (c == 0) {
+      f = sx * cy * sz * ct + st * st * sx * cx * (cy * cy * sz * sz - sy * sy * sz * sz + T(2) * cy * cy * cz * cz) +
+          T(3) * sx * cy * sz * st * invRe;
+      if (with_p) f += -sx * cy * sz * st;
+    } else if (c == 1) {
+      f = cx * sy * sz * ct + st * st * sy * cy * (cx * cx * sz * sz - sx * sx * sz * sz + T(2) * cx * cx * cz * cz) +
+          T(3) * cx * sy * sz * st * invRe;
+      if (with_p) f += -cx * sy * sz * st;
+    } else {
+      f = T(2) * cx * cy * cz * ct -
+          T(2) * st * st * sz * cz * (sx * sx * cy * cy + cx * cx * sy * sy + T(2) * cx * cx * cy * cy) +
+          T(6) * cx * cy * cz * st * invRe;
+      if (with_p) f += cx * cy * cz * st;
+    }
+    return f;
+  }
+};
+
+template <typename T>
+struct StageCoef {
+  T k1, k2, k3, k4;
+};
+
+// One RK stage for all three components; ST selects the update formula.
+template <typename T, int ST>
+__global__ void __launch_bounds__(128) stage_kernel(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
+                                                    int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot) {
+  if (forcing) {
+    fe.st = T(tr.get(sin_slot));
+    fe.ct = T(tr.get(sin_slot + 1));
+  }
+  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = 1 + blockIdx.z;
+  const long sy = g.sy(), sz = g.sz();
+  const long q = g.idx(i, j, k);
+  // The velocity set the right-hand side is computed from.
+  constexpr int in_set = (ST == kStageY2 || ST == kVelY2 || ST == kVelUStar) ? 0
+                         : (ST == kStageY3 || ST == kVelY3)                  ? 1
+                                                                             : 2;
+  const T *u = F.vel(in_set, 0), *v = F.vel(in_set, 1), *w = F.vel(in_set, 2);
+  const T *p = F.f[kP];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
+    T r = c == 0 ? rhs_u(u, v, w, q, sy, sz, co) : (c == 1 ? rhs_v(u, v, w, q, sy, sz, co) : rhs_w(u, v, w, q, sy, sz, co));
+    if (forcing) r = r + fe(c, i, j, k);
+    const long sc = c == 0 ? 1 : (c == 1 ? sy : sz);
+    if (ST == kStageY2) {
+      // src/Timestep.cpp:10-21: buf = u + a1 rhs - b grad p; buf2 = rhs   (k1 = a1, k3 = b)
+      const T gp = (ld(p, q) - ld(p, q - sc)) * co.oh[c];
+      F.vel(1, c)[q] = ld(F.vel(0, c), q) + K.k1 * r - K.k3 * gp;
+      F.vel(2, c)[q] = r;
+    } else if (ST == kStageY3) {
+      // src/Timestep.cpp:24-39: buf2 = buf + a1 rhs1 + a2 rhs2 - b grad p; u = a2 rhs2
+      const T gp = (ld(p, q) - ld(p, q - sc)) * co.oh[c];
+      const T r1 = F.vel(2, c)[q];
+      const T r2s = K.k2 * r;
+      F.vel(2, c)[q] = ld(F.vel(1, c), q) + K.k1 * r1 + r2s - K.k3 * gp;
+      F.vel(0, c)[q] = r2s;
+    } else if (ST == kStageUStar) {
+      // src/Timestep.cpp:42-54: u = buf2 - (a2 rhs2 held in u) + a3 rhs3 - b grad p   (k2 = a3, k3 = b)
+      const T gp = (ld(p, q) - ld(p, q - sc)) * co.oh[c];
+      const T r2s = -F.vel(0, c)[q];
+      F.vel(0, c)[q] = ld(F.vel(2, c), q) + r2s + K.k2 * r - K.k3 * gp;
+    } else if (ST == kVelY2) {
+      // src/TimestepVelocity.cpp:20-29: rhs_buffer = rhs; velocity_buffer = u + (dt a21) rhs
+      F.vel(2, c)[q] = r;
+      F.vel(1, c)[q] = ld(F.vel(0, c), q) + K.k1 * r;
+    } else if (ST == kVelY3) {
+      // src/TimestepVelocity.cpp:32-42 (k1 = dt, k2 = b1, k3 = a31, k4 = a32)
+      const T r1 = F.vel(2, c)[q];
+      const T uu = F.vel(0, c)[q];
+      F.vel(2, c)[q] = uu + K.k1 * (K.k2 * r1);
+      F.vel(0, c)[q] = uu + K.k1 * (K.k3 * r1 + K.k4 * r);
+    } else {
+      // src/TimestepVelocity.cpp:45-52: velocity_buffer = rhs_buffer + dt (b3 rhs)  (k1 = dt, k2 = b3)
+      const T r1 = F.vel(2, c)[q];
+      F.vel(1, c)[q] = r1 + K.k1 * (K.k2 * r);
+    }
+  }
+}
+
+// ---- boundary fill, src/VelocityTensor.cpp:36-233 ----
+
+// Sampling point of component c at index (i,j,k): staggered (face) along c.
+__device__ __forceinline__ void stag_point(const Geometry &g, int c, const long *ix, double *x) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) x[d] = d == c ? g.face(d, ix[d]) : g.node(d, ix[d]);
+}
+
+// Value the reference writes at a Dirichlet face point of component c whose
+// winning face is axis d, side s (0 min, 1 max).
+template <typename TE>
+__device__ TE face_value(const Geometry &g, int c, int d, int s, const long *pt, int kind, int fn, TE t) {
+  const TE Re = TE(g.Re);
+  if (c != d) {
+    double x[3];
+    stag_point(g, c, pt, x);
+    return analytic_vector<TE>(fn, kind, c, t, TE(x[0]), TE(x[1]), TE(x[2]), Re);
+  }
+  // Normal component: boundary value at the node plus h/2 times the exact
+  // tangential divergence (src/VelocityTensor.cpp:47-61,163-207).
+  long q[3] = {pt[0], pt[1], pt[2]};
+  q[d] = s == 0 ? 0 : g.E[d] - 1;
+  const TE xb = TE(g.node(0, q[0])), yb = TE(g.node(1, q[1])), zb = TE(g.node(2, q[2]));
+  const TE base = analytic_vector<TE>(fn, kind, c, t, xb, yb, zb, Re);
+  TE sum = TE(0);
+  bool first = true;
+#pragma unroll
+  for (int c2 = 0; c2 < 3; ++c2) {
+    if (c2 == d) continue;
+    long q1[3] = {q[0], q[1], q[2]};
+    q1[c2] += 1;
+    double x0[3], x1[3];
+    stag_point(g, c2, q1, x1);
+    stag_point(g, c2, q, x0);
+    const TE f1 = analytic_vector<TE>(fn, kind, c2, t, TE(x1[0]), TE(x1[1]), TE(x1[2]), Re);
+    const TE f0 = analytic_vector<TE>(fn, kind, c2, t, TE(x0[0]), TE(x0[1]), TE(x0[2]), Re);
+    const TE der = (f1 - f0) * TE(g.oh[c2]);
+    sum = first ? der : sum + der;
+    first = false;
+  }
+  return s == 0 ? base + TE(g.h_2[d]) * sum : base - TE(g.h_2[d]) * sum;
+}
+
+// blockIdx.z = c * 3 + d: component c, faces normal to axis d. Each face
+// point is written once, by the face the reference writes last (order
+// z_min, z_max, y_min, y_max, x_min, x_max).
+template <typename T>
+__global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int fn, TimeRef tr, int t_slot) {
+  const int c = blockIdx.z / 3, d = blockIdx.z % 3;
+  const double t = tr.get(t_slot);
+  if (g.periodic[d]) return;
+  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+  const long pa = blockIdx.x * blockDim.x + threadIdx.x;
+  const long pb = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) return;
+  T *f = c == 0 ? c0 : (c == 1 ? c1 : c2);
+  for (int s = 0; s < 2; ++s) {
+    long pt[3];
+    pt[a] = pa;
+    pt[b] = pb;
+    pt[d] = s == 0 ? 0 : g.ext(c, d) - 1;
+    bool later = false;  // an x face beats y beats z
+    for (int d2 = 0; d2 < d; ++d2)
+      if (!g.periodic[d2] && (pt[d2] == 0 || pt[d2] == g.ext(c, d2) - 1)) later = true;
+    if (later) continue;
+    const T val = T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
+    f[g.idx(pt[0], pt[1], pt[2])] = val;
+  }
+}
+
+// Periodic ghost copy along axis d for up to three fields with their own
+// extents (src/StaggeredTensor.cpp:221-257): a[0] = a[E-2], a[E-1] = a[1].
+template <typename T>
+__global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int d, int scalar) {
+  const int c = blockIdx.z;
+  T *f = c == 0 ? f0 : (c == 1 ? f1 : f2);
+  if (!f) return;
+  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+  auto ext = [&](int ax) { return scalar ? g.E[ax] : g.ext(c, ax); };
+  const long pa = blockIdx.x * blockDim.x + threadIdx.x;
+  const long pb = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pa >= ext(a) || pb >= ext(b)) return;
+  long lo[3], hi[3], src_lo[3], src_hi[3];
+  lo[a] = hi[a] = src_lo[a] = src_hi[a] = pa;
+  lo[b] = hi[b] = src_lo[b] = src_hi[b] = pb;
+  const int E = ext(d);
+  lo[d] = 0;
+  src_lo[d] = E - 2;
+  hi[d] = E - 1;
+  src_hi[d] = 1;
+  f[g.idx(lo[0], lo[1], lo[2])] = f[g.idx(src_lo[0], src_lo[1], src_lo[2])];
+  f[g.idx(hi[0], hi[1], hi[2])] = f[g.idx(src_hi[0], src_hi[1], src_hi[2])];
+}
+
+// ---- Poisson right-hand side and projection ----
+
+template <typename T>
+__global__ void divergence_kernel(Geometry g, T *phi, const T *u, const T *v, const T *w, T inv_dt) {
+  const int i = g.own_lo[0] + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = g.own_lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = g.own_lo[2] + blockIdx.z;
+  if (i >= g.own_lo[0] + g.np[0] || j >= g.own_lo[1] + g.np[1]) return;
+  const long q = g.idx(i, j, k);
+  const T du = (ld(u, q + 1) - ld(u, q)) * T(g.oh[0]);
+  const T dv = (ld(v, q + g.sy()) - ld(v, q)) * T(g.oh[1]);
+  const T dw = (ld(w, q + g.sz()) - ld(w, q)) * T(g.oh[2]);
+  phi[q] = (du + dv + dw) * inv_dt;
+}
+
+template <typename T>
+__global__ void neumann_flux_serial_kernel(Geometry g, T *phi, int kind, TimeRef tr, int slot_new, int slot_old) {
+  const double t_new = tr.get(slot_new), t_old = tr.get(slot_old);
+  // Every boundary node is visited by one thread, which adds the terms of all
+  // faces containing it in the reference's order (z, then y, then x).
+  const long n_total = (long)g.E[0] * g.E[1] * g.E[2];
+  const long id = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= n_total) return;
+  const long i = id % g.E[0], j = (id / g.E[0]) % g.E[1], k = id / ((long)g.E[0] * g.E[1]);
+  const bool onb = i == 0 || i == g.E[0] - 1 || j == 0 || j == g.E[1] - 1 || k == 0 || k == g.E[2] - 1;
+  if (!onb) return;
+  const double x = g.node(0, i), y = g.node(1, j), z = g.node(2, k);
+  auto G = [&](int c) {
+    return T(analytic_pressure_gradient<T>(kind, c, T(t_old), T(x), T(y), T(z), T(g.Re)) -
+             analytic_pressure_gradient<T>(kind, c, T(t_new), T(x), T(y), T(z), T(g.Re)));
+  };
+  const long q = g.idx(i, j, k);
+  T r = phi[q];
+  if (k == 0) r += G(2) * T(2.0) * T(g.oh[2]);
+  if (k == g.E[2] - 1) r -= G(2) * T(2.0) * T(g.oh[2]);
+  if (j == 0) r += G(1) * T(2.0) * T(g.oh[1]);
+  if (j == g.E[1] - 1) r -= G(1) * T(2.0) * T(g.oh[1]);
+  if (i == 0) r += G(0) * T(2.0) * T(g.oh[0]);
+  if (i == g.E[0] - 1) r -= G(0) * T(2.0) * T(g.oh[0]);
+  phi[q] = r;
+}
+
+template <typename T>
+__global__ void project_kernel(Geometry g, T *p, const T *phi, T *u, T *v, T *w, T dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  const long q = g.idx(i, j, k);
+  if (i < g.E[0] && j < g.E[1] && k < g.E[2]) p[q] = p[q] + ld(phi, q);
+  T *vel[3] = {u, v, w};
+  const long sc[3] = {1, g.sy(), g.sz()};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
+    const T gp = (ld(phi, q) - ld(phi, q - sc[c])) * T(g.oh[c]);
+    vel[c][q] = vel[c][q] - gp * dt;
+  }
+}
+
+// ---- layout conversion and initial fields ----
+
+template <typename T>
+__global__ void scatter_kernel(Geometry g, T *dst, const double *src, int ex, int ey, int ez) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= ex || j >= ey) return;
+  dst[g.idx(i, j, k)] = T(src[i + (long)ex * (j + (long)ey * k)]);
+}
+
+template <typename T>
+__global__ void gather_kernel(Geometry g, double *dst, const T *src, int ex, int ey, int ez) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= ex || j >= ey) return;
+  dst[i + (long)ex * (j + (long)ey * k)] = double(src[g.idx(i, j, k)]);
+}
+
+template <typename T>
+__global__ void set_exact_kernel(Geometry g, T *f, int comp, int kind, double t, int ex, int ey) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= ex || j >= ey) return;
+  const long pt[3] = {i, j, k};
+  double x[3];
+  stag_point(g, comp, pt, x);  // comp 3 (pressure): every axis at nodes
+  f[g.idx(i, j, k)] = T(analytic_value<double>(kind, comp, t, x[0], x[1], x[2], g.Re));
+}
+
+// ---- double-precision reductions ----
+
+__device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
+  // Non-negative IEEE doubles order like their bit patterns.
+  atomicMax(reinterpret_cast<unsigned long long *>(addr), __double_as_longlong(v));
+}
+
+template <int NT>
+__device__ void block_reduce3(double a, double b, double m, double *acc) {
+  __shared__ double sa[NT / 32], sb[NT / 32], sm[NT / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sa[wid] = a, sb[wid] = b, sm[wid] = m;
+  __syncthreads();
+  if (wid == 0) {
+    a = lane < NT / 32 ? sa[lane] : 0.0;
+    b = lane < NT / 32 ? sb[lane] : 0.0;
+    m = lane < NT / 32 ? sm[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    }
+    if (lane == 0) {
+      atomicAdd(acc + 0, a);
+      atomicAdd(acc + 1, b);
+      atomic_max_nonneg(acc + 2, m);
+    }
+  }
+}
+
+// src/Norms.cpp:11-47: velocity interpolated to interior nodes vs the family.
+template <typename T>
+__global__ void __launch_bounds__(256) velocity_error_kernel(Geometry g, const T *u, const T *v, const T *w, int kind,
+                                                             int fn, double t, double *acc) {
+  const long ni = g.E[0] - 2, nj = g.E[1] - 2, nk = g.E[2] - 2;
+  const long n = ni * nj * nk;
+  double a = 0, b = 0, m = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+    const long i = 1 + id % ni, j = 1 + (id / ni) % nj, k = 1 + id / (ni * nj);
+    const long q = g.idx(i, j, k);
+    const double x = g.origin[0] + (double)(g.base[0] + i) * g.h[0];
+    const double y = g.origin[1] + (double)(g.base[1] + j) * g.h[1];
+    const double z = g.origin[2] + (double)(g.base[2] + k) * g.h[2];
+    const double iu = ((double)u[q] + (double)u[q + 1]) / 2.0;
+    const double iv = ((double)v[q] + (double)v[q + g.sy()]) / 2.0;
+    const double iw = ((double)w[q] + (double)w[q + g.sz()]) / 2.0;
+    const double eu = analytic_vector<double>(fn, kind, 0, t, x, y, z, g.Re) - iu;
+    const double ev = analytic_vector<double>(fn, kind, 1, t, x, y, z, g.Re) - iv;
+    const double ew = analytic_vector<double>(fn, kind, 2, t, x, y, z, g.Re) - iw;
+    a += sqrt(eu * eu + ev * ev + ew * ew);
+    b += eu * eu + ev * ev + ew * ew;
+    m = fmax(m, fmax(fmax(fabs(eu), fabs(ev)), fabs(ew)));
+  }
+  block_reduce3<256>(a, b, m, acc);
+}
+
+// src/Norms.cpp:78-92: pressure on owner points vs the family.
+template <typename T>
+__global__ void __launch_bounds__(256) pressure_error_kernel(Geometry g, const T *p, int kind, double t, double *acc) {
+  const long ni = g.np[0], nj = g.np[1], nk = g.np[2];
+  const long n = ni * nj * nk;
+  double a = 0, b = 0, m = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+    const long i = g.own_lo[0] + id % ni, j = g.own_lo[1] + (id / ni) % nj, k = g.own_lo[2] + id / (ni * nj);
+    const double x = g.origin[0] + (double)(g.base[0] + i) * g.h[0];
+    const double y = g.origin[1] + (double)(g.base[1] + j) * g.h[1];
+    const double z = g.origin[2] + (double)(g.base[2] + k) * g.h[2];
+    const double e = analytic_value<double>(kind, 3, t, x, y, z, g.Re) - (double)p[g.idx(i, j, k)];
+    a += fabs(e);
+    b += e * e;
+    m = fmax(m, fabs(e));
+  }
+  block_reduce3<256>(a, b, m, acc);
+}
+
+// src/PressureEquation.cpp:294-297: sum of (exact - p) over owner points.
+template <typename T>
+__global__ void __launch_bounds__(256) pressure_diff_kernel(Geometry g, const T *p, int kind, double t, double *acc) {
+  const long ni = g.np[0], nj = g.np[1], nk = g.np[2];
+  const long n = ni * nj * nk;
+  double a = 0;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+    const long i = g.own_lo[0] + id % ni, j = g.own_lo[1] + (id / ni) % nj, k = g.own_lo[2] + id / (ni * nj);
+    a += analytic_value<double>(kind, 3, t, g.node(0, i), g.node(1, j), g.node(2, k), g.Re) - (double)p[g.idx(i, j, k)];
+  }
+  block_reduce3<256>(a, 0.0, 0.0, acc);
+}
+
+// src/PressureEquation.cpp:335-342: p += mean difference, every point.
+template <typename T>
+__global__ void add_shift_kernel(Geometry g, T *p, const double *acc, double count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= g.E[0] || j >= g.E[1]) return;
+  const double shift = acc[0] / count;
+  const long q = g.idx(i, j, k);
+  p[q] = T((double)p[q] + shift);
+}
+
+template <typename T>
+__global__ void pressure_gradient_kernel(Geometry g, T *u, T *v, T *w, const T *p) {
+  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = 1 + blockIdx.z;
+  T *vel[3] = {u, v, w};
+  const long sc[3] = {1, g.sy(), g.sz()};
+  const long q = g.idx(i, j, k);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
+    vel[c][q] = (p[q] - p[q - sc[c]]) * T(g.oh[c]);
+  }
+}
+
+template <typename T>
+__global__ void nonfinite_kernel(const T *f, long n, int *flag) {
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x)
+    if (!isfinite(f[id])) {
+      *flag = 1;
+      return;
+    }
+}
+
+inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+template <typename T>
+Coeffs<T> make_coeffs(const Geometry &g) {
+  Coeffs<T> c;
+  for (int d = 0; d < 3; ++d) {
+    c.o2h[d] = T(g.o2h[d]);
+    c.o8h[d] = T(g.o8h[d]);
+    c.oh2Re[d] = T(g.oh2Re[d]);
+    c.oh[d] = T(g.oh[d]);
+  }
+  return c;
+}
+
+}  // namespace
+
+// ---- launchers ----
+
+template <typename T>
+void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
+                  const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches) {
+  const dim3 blk(32, 4, 1);
+  const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
+  const dim3 grid(cdiv(ni - 2, 32), cdiv(g.Es[1] - 2, 4), (unsigned)(g.Es[2] - 2));
+  const double dt = sc.dt;
+  StageCoef<T> K{};
+  switch (st) {
+    case kStageY2: {
+      const double a1 = 64.0 / 120.0 * dt;
+      K = {T(a1), T(0), T(a1), T(0)};
+      break;
+    }
+    case kStageY3: {
+      const double a1 = -34.0 / 120.0 * dt, a2 = 50.0 / 120.0 * dt;
+      K = {T(a1), T(a2), T(a1 + a2), T(0)};
+      break;
+    }
+    case kStageUStar: {
+      const double a2 = -50.0 / 120.0 * dt, a3 = 90.0 / 120.0 * dt;
+      K = {T(0), T(a3), T(a2 + a3), T(0)};
+      break;
+    }
+    case kVelY2: {
+      const double a21 = (8.0 / 15.0);
+      K = {T(dt * a21), T(0), T(0), T(0)};
+      break;
+    }
+    case kVelY3: {
+      K = {T(dt), T(1.0 / 4.0), T(1.0 / 4.0), T(5.0 / 12.0)};
+      break;
+    }
+    default: {
+      K = {T(dt), T(3.0 / 4.0), T(0), T(0)};
+      break;
+    }
+  }
+  ForcingEval<T> fe{};
+  fe.tab = ft.tab;
+  fe.maxE = ft.maxE;
+  fe.st = T(0);
+  fe.ct = T(0);
+  fe.invRe = T(1.0 / g.Re);
+  fe.with_p = sc.forcing == 2;
+  const int forcing = sc.forcing != 0 && field_kind == kFieldSincos && ft.tab != nullptr;
+  const Coeffs<T> co = make_coeffs<T>(g);
+  switch (st) {
+    case kStageY2: stage_kernel<T, kStageY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+    case kStageY3: stage_kernel<T, kStageY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+    case kStageUStar: stage_kernel<T, kStageUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+    case kVelY2: stage_kernel<T, kVelY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+    case kVelY3: stage_kernel<T, kVelY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+    default: stage_kernel<T, kVelUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+  }
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn, TimeRef tr, int t_slot,
+                     cudaStream_t s, long long *launches) {
+  const dim3 blk(32, 8, 1);
+  int mx = 0;
+  for (int d = 0; d < 3; ++d) mx = mx > g.Es[d] ? mx : g.Es[d];
+  if (!(g.periodic[0] && g.periodic[1] && g.periodic[2])) {
+    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 9);
+    bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot);
+    if (launches) ++*launches;
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (!g.periodic[d]) continue;
+    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 3);
+    periodic_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], d, 0);
+    if (launches) ++*launches;
+  }
+}
+
+template <typename T>
+void launch_periodic_scalar(const Geometry &g, T *f, cudaStream_t s, long long *launches) {
+  const dim3 blk(32, 8, 1);
+  int mx = 0;
+  for (int d = 0; d < 3; ++d) mx = mx > g.E[d] ? mx : g.E[d];
+  for (int d = 0; d < 3; ++d) {
+    if (!g.periodic[d]) continue;
+    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 1);
+    periodic_kernel<T><<<grid, blk, 0, s>>>(g, f, nullptr, nullptr, d, 1);
+    if (launches) ++*launches;
+  }
+}
+
+template <typename T>
+void launch_divergence(const Geometry &g, T *phi, T *const vel[3], double dt, cudaStream_t s, long long *launches) {
+  const dim3 blk(32, 4, 1);
+  const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), (unsigned)g.np[2]);
+  divergence_kernel<T><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt));
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_neumann_flux(const Geometry &g, T *phi, int field_kind, TimeRef tr, int slot_new, int slot_old,
+                         cudaStream_t s, long long *launches) {
+  const long n = (long)g.E[0] * g.E[1] * g.E[2];
+  neumann_flux_serial_kernel<T><<<cdiv(n, 256), 256, 0, s>>>(g, phi, field_kind, tr, slot_new, slot_old);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, cudaStream_t s,
+                    long long *launches) {
+  const dim3 blk(32, 4, 1);
+  const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
+  const dim3 grid(cdiv(ni, 32), cdiv(g.Es[1], 4), (unsigned)g.Es[2]);
+  project_kernel<T><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt));
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_scatter(const Geometry &g, T *dst, const double *src, int ex, int ey, int ez, cudaStream_t s,
+                    long long *launches) {
+  const dim3 blk(32, 8, 1), grid(cdiv(ex, 32), cdiv(ey, 8), (unsigned)ez);
+  scatter_kernel<T><<<grid, blk, 0, s>>>(g, dst, src, ex, ey, ez);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_gather(const Geometry &g, double *dst, const T *src, int ex, int ey, int ez, cudaStream_t s,
+                   long long *launches) {
+  const dim3 blk(32, 8, 1), grid(cdiv(ex, 32), cdiv(ey, 8), (unsigned)ez);
+  gather_kernel<T><<<grid, blk, 0, s>>>(g, dst, src, ex, ey, ez);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_set_exact(const Geometry &g, T *f, int comp, int field_kind, double t, cudaStream_t s,
+                      long long *launches) {
+  const int ex = comp < 3 ? g.ext(comp, 0) : g.E[0];
+  const int ey = comp < 3 ? g.ext(comp, 1) : g.E[1];
+  const int ez = comp < 3 ? g.ext(comp, 2) : g.E[2];
+  const dim3 blk(32, 8, 1), grid(cdiv(ex, 32), cdiv(ey, 8), (unsigned)ez);
+  set_exact_kernel<T><<<grid, blk, 0, s>>>(g, f, comp, field_kind, t, ex, ey);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_pressure_mean_diff(const Geometry &g, const T *p, int field_kind, double t, double *acc, cudaStream_t s,
+                               long long *launches) {
+  pressure_diff_kernel<T><<<1024, 256, 0, s>>>(g, p, field_kind, t, acc);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_add_scalar(const Geometry &g, T *p, const double *shift, cudaStream_t s, long long *launches) {
+  const dim3 blk(32, 8, 1), grid(cdiv(g.E[0], 32), cdiv(g.E[1], 8), (unsigned)g.E[2]);
+  const double count = (double)((size_t)g.np[0] * (size_t)g.np[1] * (size_t)g.np[2]);
+  add_shift_kernel<T><<<grid, blk, 0, s>>>(g, p, shift, count);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_velocity_errors(const Geometry &g, T *const vel[3], int field_kind, int fn, double t, double *acc,
+                            cudaStream_t s, long long *launches) {
+  velocity_error_kernel<T><<<1024, 256, 0, s>>>(g, vel[0], vel[1], vel[2], field_kind, fn, t, acc);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_pressure_errors(const Geometry &g, const T *p, int field_kind, double t, double *acc, cudaStream_t s,
+                            long long *launches) {
+  pressure_error_kernel<T><<<1024, 256, 0, s>>>(g, p, field_kind, t, acc);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_pressure_gradient(const Geometry &g, T *const vel[3], const T *p, cudaStream_t s, long long *launches) {
+  const dim3 blk(32, 4, 1);
+  const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
+  const dim3 grid(cdiv(ni - 2, 32), cdiv(g.Es[1] - 2, 4), (unsigned)(g.Es[2] - 2));
+  pressure_gradient_kernel<T><<<grid, blk, 0, s>>>(g, vel[0], vel[1], vel[2], p);
+  if (launches) ++*launches;
+}
+
+template <typename T>
+void launch_nonfinite_check(const T *f, long n, int *flag, cudaStream_t s, long long *launches) {
+  nonfinite_kernel<T><<<1024, 256, 0, s>>>(f, n, flag);
+  if (launches) ++*launches;
+}
+
+#define MIFGPU_INSTANTIATE(T)                                                                                        \
+  template void launch_stage<T>(const Geometry &, const Fields<T> &, StageKind, const StageScalars<T> &,             \
+                                const ForcingTables<T> &, int, TimeRef, cudaStream_t, long long *);                  \
+  template void launch_apply_bc<T>(const Geometry &, T *const[3], int, int, TimeRef, int, cudaStream_t, long long *); \
+  template void launch_periodic_scalar<T>(const Geometry &, T *, cudaStream_t, long long *);                       \
+  template void launch_divergence<T>(const Geometry &, T *, T *const[3], double, cudaStream_t, long long *);       \
+  template void launch_neumann_flux<T>(const Geometry &, T *, int, TimeRef, int, int, cudaStream_t, long long *);  \
+  template void launch_project<T>(const Geometry &, T *, const T *, T *const[3], double, cudaStream_t, long long *); \
+  template void launch_scatter<T>(const Geometry &, T *, const double *, int, int, int, cudaStream_t, long long *); \
+  template void launch_gather<T>(const Geometry &, double *, const T *, int, int, int, cudaStream_t, long long *);  \
+  template void launch_set_exact<T>(const Geometry &, T *, int, int, double, cudaStream_t, long long *);           \
+  template void launch_pressure_mean_diff<T>(const Geometry &, const T *, int, double, double *, cudaStream_t,     \
+                                             long long *);                                                         \
+  template void launch_add_scalar<T>(const Geometry &, T *, const double *, cudaStream_t, long long *);            \
+  template void launch_velocity_errors<T>(const Geometry &, T *const[3], int, int, double, double *, cudaStream_t, \
+                                          long long *);                                                            \
+  template void launch_pressure_errors<T>(const Geometry &, const T *, int, double, double *, cudaStream_t,        \
+                                          long long *);                                                            \
+  template void launch_pressure_gradient<T>(const Geometry &, T *const[3], const T *, cudaStream_t, long long *);  \
+  template void launch_nonfinite_check<T>(const T *, long, int *, cudaStream_t, long long *);
+
+}  // namespace mifgpu

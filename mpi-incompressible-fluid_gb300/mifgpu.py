@@ -1,0 +1,236 @@
+"""Python host binding of the mifgpu C ABI (include/mifgpu.h) over ctypes.
+
+It mirrors the reference's operator interface for the time step
+(include/Timestep.h:16-27, include/TimestepVelocity.h:15-16,
+include/PressureEquation.h:10-25, include/Norms.h): one ``Solver`` holds what
+the reference passes as Constants, PressureSolverStructures and the six
+tensors, and exposes ``timestep``, ``timestep_nhn``, ``timestep_velocity``,
+``solve_pressure_equation_homogeneous_periodic``, ``apply_bc``,
+``adjust_pressure`` and the error norms. Fields travel as numpy arrays in the
+reference's layout: shape (Ez, Ey, Ex), x fastest.
+
+There is no CPU path: if libmifgpu.so is missing or no CUDA device is present,
+constructing a Solver raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmifgpu.so")
+
+FIELDS = {"u": 0, "v": 1, "w": 2, "u1": 3, "v1": 4, "w1": 5, "u2": 6, "v2": 7, "w2": 8, "p": 9, "phi": 10}
+FP64, MIXED = 0, 1
+FIELD_ZERO, FIELD_SINCOS, FIELD_ETHIER = 0, 1, 2
+FORCING_NONE, FORCING_VELOCITY, FORCING_NAVIER_STOKES = 0, 1, 2
+
+EXPORTED = [
+    "mifgpu_create", "mifgpu_destroy", "mifgpu_set_stream", "mifgpu_synchronize", "mifgpu_last_error",
+    "mifgpu_field_extent", "mifgpu_upload", "mifgpu_download", "mifgpu_set_exact_velocity",
+    "mifgpu_set_exact_pressure", "mifgpu_timestep", "mifgpu_run", "mifgpu_timestep_host", "mifgpu_timestep_nhn",
+    "mifgpu_timestep_velocity", "mifgpu_apply_bc", "mifgpu_solve_pressure", "mifgpu_divergence", "mifgpu_project",
+    "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_launch_count", "mifgpu_device_bytes",
+]
+
+
+class MifGpuError(RuntimeError):
+    pass
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("n_global", C.c_long * 3),
+        ("size", C.c_double * 3),
+        ("origin", C.c_double * 3),
+        ("Re", C.c_double),
+        ("dt", C.c_double),
+        ("periodic", C.c_int * 3),
+        ("precision", C.c_int),
+        ("boundary_kind", C.c_int),
+        ("forcing", C.c_int),
+    ]
+
+
+_LIB = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libmifgpu.so (built by build.py) and declare its signatures."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise MifGpuError(f"mifgpu CUDA library not built: {path} (run build.py)")
+    lib = C.CDLL(path)
+    vp, i, d, dp = C.c_void_p, C.c_int, C.c_double, C.c_void_p
+    sig = {
+        "mifgpu_create": [C.POINTER(Params), C.POINTER(C.c_void_p)],
+        "mifgpu_destroy": [vp],
+        "mifgpu_set_stream": [vp, vp],
+        "mifgpu_synchronize": [vp],
+        "mifgpu_field_extent": [vp, i, dp],
+        "mifgpu_upload": [vp, i, dp],
+        "mifgpu_download": [vp, i, dp],
+        "mifgpu_set_exact_velocity": [vp, i, d],
+        "mifgpu_set_exact_pressure": [vp, d],
+        "mifgpu_timestep": [vp, d],
+        "mifgpu_run": [vp, d, i],
+        "mifgpu_timestep_host": [vp, d, dp, dp, dp, dp],
+        "mifgpu_timestep_nhn": [vp, d],
+        "mifgpu_timestep_velocity": [vp, d],
+        "mifgpu_apply_bc": [vp, i, d],
+        "mifgpu_solve_pressure": [vp, i, d],
+        "mifgpu_divergence": [vp, i, d],
+        "mifgpu_project": [vp, i, d],
+        "mifgpu_adjust_pressure": [vp, d],
+        "mifgpu_error_norms": [vp, d, dp],
+        "mifgpu_launch_count": [vp, dp],
+        "mifgpu_device_bytes": [vp, dp],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.mifgpu_last_error.argtypes = [vp]
+    lib.mifgpu_last_error.restype = C.c_char_p
+    _LIB = lib
+    return lib
+
+
+class Solver:
+    """One device-resident solver state (the reference's Constants + tensors)."""
+
+    def __init__(self, n_global, size=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), Re=1000.0, dt=1e-4,
+                 periodic=(False, False, False), precision=FP64, boundary_kind=FIELD_ZERO, forcing=FORCING_NONE):
+        self.lib = load_library()
+        p = Params()
+        for k in range(3):
+            p.n_global[k] = int(n_global[k])
+            p.size[k] = float(size[k])
+            p.origin[k] = float(origin[k])
+            p.periodic[k] = 1 if periodic[k] else 0
+        p.Re, p.dt = float(Re), float(dt)
+        p.precision, p.boundary_kind, p.forcing = int(precision), int(boundary_kind), int(forcing)
+        self.params = p
+        self.dt = float(dt)
+        h = C.c_void_p()
+        rc = self.lib.mifgpu_create(C.byref(p), C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.lib.mifgpu_last_error(h).decode() if h.value else "no context"
+            if h.value:
+                self.lib.mifgpu_destroy(h)
+            self.h = None
+            raise MifGpuError(f"mifgpu_create failed ({rc}): {msg}")
+
+    # -- plumbing --
+    def _check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            raise MifGpuError(f"{what} failed ({rc}): {self.lib.mifgpu_last_error(self.h).decode()}")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mifgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(self.lib.mifgpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def synchronize(self) -> None:
+        self._check(self.lib.mifgpu_synchronize(self.h), "synchronize")
+
+    def launch_count(self) -> int:
+        out = C.c_longlong(0)
+        self._check(self.lib.mifgpu_launch_count(self.h, C.byref(out)), "launch_count")
+        return out.value
+
+    def device_bytes(self) -> int:
+        out = C.c_size_t(0)
+        self._check(self.lib.mifgpu_device_bytes(self.h, C.byref(out)), "device_bytes")
+        return out.value
+
+    # -- fields --
+    def extent(self, name: str) -> tuple:
+        out = (C.c_long * 3)()
+        self._check(self.lib.mifgpu_field_extent(self.h, FIELDS[name], out), "field_extent")
+        return tuple(out)
+
+    def shape(self, name: str) -> tuple:
+        ex, ey, ez = self.extent(name)
+        return (ez, ey, ex)
+
+    def upload(self, name: str, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.shape != self.shape(name):
+            raise MifGpuError(f"field {name}: shape {a.shape} != {self.shape(name)}")
+        self._check(self.lib.mifgpu_upload(self.h, FIELDS[name], a.ctypes.data), "upload")
+        self.synchronize()
+
+    def download(self, name: str) -> np.ndarray:
+        out = np.empty(self.shape(name), dtype=np.float64)
+        self._check(self.lib.mifgpu_download(self.h, FIELDS[name], out.ctypes.data), "download")
+        return out
+
+    def set_exact_velocity(self, vset: int, t: float) -> None:
+        self._check(self.lib.mifgpu_set_exact_velocity(self.h, vset, t), "set_exact_velocity")
+
+    def set_exact_pressure(self, t: float) -> None:
+        self._check(self.lib.mifgpu_set_exact_pressure(self.h, t), "set_exact_pressure")
+
+    def load_state(self, st: dict) -> None:
+        for n, a in st.items():
+            self.upload(n, a)
+
+    def state(self, names=tuple(FIELDS)) -> dict:
+        return {n: self.download(n) for n in names}
+
+    # -- the reference's operators --
+    def timestep(self, t_n: float) -> None:
+        self._check(self.lib.mifgpu_timestep(self.h, t_n), "timestep")
+
+    def run(self, t0: float, nsteps: int) -> None:
+        self._check(self.lib.mifgpu_run(self.h, t0, nsteps), "run")
+
+    def timestep_host(self, t_n: float, u: np.ndarray, v: np.ndarray, w: np.ndarray, p: np.ndarray) -> None:
+        for a in (u, v, w, p):
+            if not (a.flags.c_contiguous and a.dtype == np.float64):
+                raise MifGpuError("timestep_host needs C-contiguous float64 arrays")
+        self._check(self.lib.mifgpu_timestep_host(self.h, t_n, u.ctypes.data, v.ctypes.data, w.ctypes.data,
+                                                  p.ctypes.data), "timestep_host")
+
+    def timestep_nhn(self, t_n: float) -> None:
+        self._check(self.lib.mifgpu_timestep_nhn(self.h, t_n), "timestep_nhn")
+
+    def timestep_velocity(self, t_n: float) -> None:
+        self._check(self.lib.mifgpu_timestep_velocity(self.h, t_n), "timestep_velocity")
+
+    def apply_bc(self, vset: int, t: float) -> None:
+        self._check(self.lib.mifgpu_apply_bc(self.h, vset, t), "apply_bc")
+
+    def solve_pressure_equation_homogeneous_periodic(self, vset: int, dt: float) -> None:
+        self._check(self.lib.mifgpu_solve_pressure(self.h, vset, dt), "solve_pressure")
+
+    solve_pressure = solve_pressure_equation_homogeneous_periodic
+
+    def divergence(self, vset: int, dt: float) -> None:
+        self._check(self.lib.mifgpu_divergence(self.h, vset, dt), "divergence")
+
+    def project(self, vset: int, dt: float) -> None:
+        self._check(self.lib.mifgpu_project(self.h, vset, dt), "project")
+
+    def adjust_pressure(self, t: float) -> None:
+        self._check(self.lib.mifgpu_adjust_pressure(self.h, t), "adjust_pressure")
+
+    def error_norms(self, t: float) -> np.ndarray:
+        out = np.zeros(9)
+        self._check(self.lib.mifgpu_error_norms(self.h, t, out.ctypes.data), "error_norms")
+        return out

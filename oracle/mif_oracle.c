@@ -711,3 +711,12 @@ int mif_oracle_error_norms(void *h, double t, double out[9]) {
   for (int c = 0; c < 3; ++c) free(G[c].a);
   return 0;
 }
+
+/* Point evaluations of the analytic families, for formula checks. */
+double mif_oracle_forcing_value(int kind, int comp, double t, double x, double y, double z, double Re, int with_p) {
+  return mf_forcing(kind, comp, t, x, y, z, Re, with_p);
+}
+
+double mif_oracle_pressure_gradient_value(int kind, int comp, double t, double x, double y, double z, double Re) {
+  return mf_pressure_gradient(kind, comp, t, x, y, z, Re);
+}

@@ -51,6 +51,8 @@ int mif_oracle_solve_pressure_nhn(void *h, int set, double dt, double t_new, dou
 int mif_oracle_apply_bc(void *h, int set, double t);
 int mif_oracle_adjust_pressure(void *h, double t);
 int mif_oracle_error_norms(void *h, double t, double out[9]);
+double mif_oracle_forcing_value(int kind, int comp, double t, double x, double y, double z, double Re, int with_p);
+double mif_oracle_pressure_gradient_value(int kind, int comp, double t, double x, double y, double z, double Re);
 
 #ifdef __cplusplus
 }
