@@ -9,12 +9,13 @@ from __future__ import annotations
 import concurrent.futures as cf
 import glob
 import os
+import platform
 import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", platform.machine())
 LIB = os.path.join(HERE, "libmifgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
@@ -56,11 +57,14 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(sources), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, sources))
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
+    stamp = os.path.join(BUILD, "lib.stamp")
+    if not os.path.exists(LIB) or not os.path.exists(stamp) or os.path.getmtime(stamp) < _newest(objs):
         cmd = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+        with open(stamp, "w") as f:
+            f.write(platform.machine() + "\n")
     return LIB
 
 
