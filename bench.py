@@ -1,0 +1,398 @@
+"""Throughput of one GB300 projection step (Gcell-steps/s), JSON on one line.
+
+Workload (default): the manufactured-solution unit cube at 512^3 cells
+(513^3 nodes, every face Dirichlet, homogeneous-Neumann DCT-I Poisson),
+Re = 1000, dt = 1e-4 (64/512)^2 (dt scaled with h^2 as in the large
+manufactured runs), SINCOS velocity with its Navier-Stokes forcing, mixed
+precision (f32 storage and stencils, f64 eigenvalue division). Inputs are the
+analytic fields at t = 0, generated on the device (synthetic; no dataset).
+
+Arms:
+  --impl gb300      (default) the CUDA library: `value` from CUDA events around
+                    K graph-replayed steps with the fields resident in HBM;
+                    `e2e` through the drop-in host call mifgpu_timestep_host
+                    (pinned host buffers in the reference layout, H2D + step +
+                    D2H inside the timed region); `roofline` of the dominant
+                    kernel class; `cpu_baseline` of the oracle on a bounded sample.
+  --impl reference  the reference's CPU algorithm (the bit-exact C restatement
+                    under oracle/, since the reference library itself cannot be
+                    rebuilt without its sources) on every host core, one
+                    independent replica per core, on a bounded sample.
+Multi-GPU: the path does not shard; N ranks run N independent replicas
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "mpi-incompressible-fluid_gb300")
+ORACLE_DIR = os.path.join(REPO, "oracle")
+for _p in (PKG, ORACLE_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "full-step Gcell/s at 512³, mixed vs FP64 at matched L∞ err; adjoint/fwd ratio"
+UNIT = "Gcell-steps/s"
+
+WORKLOADS = {
+    # name: (n_global, size, origin, periodic, Re, dt, kind, forcing)
+    "cube512": ((513, 513, 513), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
+                1e-4 * (64.0 / 512.0) ** 2, 1, 2),
+    "channel512x256x512": ((513, 257, 513), (4 * 3.141592653589793, 2.0, 2 * 3.141592653589793), (0.0, 0.0, 0.0),
+                           (True, False, True), 5000.0, 5e-4, 0, 0),
+    "cube64": ((65, 65, 65), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0, 1e-4, 1, 2),
+}
+
+# Algorithmic HBM sweeps (full-field reads + writes) per launch of each kernel
+# class; times the field bytes and the cell count give algorithmic bytes.
+SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 2.0, "y_forward": 2.0, "z_fused": 2.0,
+          "y_inverse": 2.0, "x_inverse": 2.0, "project": 9.0}
+LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3, "z_fused": 3, "y_inverse": 3,
+                     "x_inverse": 3, "project": 3}
+STEP_SWEEPS = 90.0  # per step: 33 stage + 3 x (4 + 5 x 2 + 9) Poisson/projection, minus fusions not done
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU baseline
+
+def _cpu_worker(args):
+    n, steps, periodic, size, Re, dt, kind = args
+    import oracle as O
+
+    case = O.Case(n_global=(n, n, n), size=size, Re=Re, dt=dt, periodic=periodic, exact_kind=kind, forcing=2)
+    s = O.OracleSolver(case)
+    s.set_exact_velocity(0, 0.0, True)
+    s.set_exact_pressure(0.0)
+    s.timestep(0.0)  # warm-up
+    t0 = time.perf_counter()
+    for k in range(steps):
+        s.timestep((k + 1) * dt)
+    el = time.perf_counter() - t0
+    return case.cells() * steps, el
+
+
+def cpu_baseline(workers: int, n: int = 97, steps: int = 3):
+    """The oracle (bit-exact restatement of the reference's step) on a bounded
+    sample of the same workload family: an n^3-node manufactured cube,
+    `steps` timed steps per worker, one worker per core."""
+    import multiprocessing as mp
+
+    import oracle as O
+
+    O.build(with_ref=False)
+    w = WORKLOADS["cube512"]
+    job = (n, steps, w[3], w[1], w[4], w[5], w[6])
+    t0 = time.perf_counter()
+    if workers == 1:
+        res = [_cpu_worker(job)]
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers) as pool:
+            res = pool.map(_cpu_worker, [job] * workers)
+    wall = time.perf_counter() - t0
+    cells = sum(r[0] for r in res)
+    per_worker = max(r[1] for r in res)
+    return {"value": cells / per_worker / 1e9, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{n - 1}^3-cell manufactured cube (SINCOS + NS forcing), {steps} steps per core after "
+                      f"1 warm-up, {workers} independent replicas, oracle/mif_oracle.c built -O2 "
+                      f"(wall {wall:.1f}s)"}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args):
+    import torch
+
+    import mifgpu
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    import build as pkg_build
+
+    pkg_build.build()
+    n_global, size, origin, periodic, Re, dt, kind, forcing = WORKLOADS[args.workload]
+    prec = mifgpu.MIXED if args.precision == "mixed" else mifgpu.FP64
+    s = mifgpu.Solver(n_global=n_global, size=size, origin=origin, Re=Re, dt=dt, periodic=periodic,
+                      precision=prec, boundary_kind=kind, forcing=forcing)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    s.set_exact_velocity(0, 0.0)
+    s.set_exact_pressure(0.0)
+    s.synchronize()
+    cells = 1
+    for n, p in zip(n_global, periodic):
+        cells *= (n - 1)
+    elem = 4 if prec == mifgpu.MIXED else 8
+
+    # warm-up (graph capture happens here)
+    t = 0.0
+    s.run(t, args.warmup)
+    t += args.warmup * dt
+    torch.cuda.synchronize()
+
+    launches0 = s.launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        s.run(t, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    t += args.steps * dt
+    ms = e0.elapsed_time(e1)
+    ms = allreduce_max(ms, world)
+    launches = s.launch_count() - launches0
+    value = world * cells * args.steps / (ms / 1e3) / 1e9
+
+    # error against the analytic solution after the run (matched-error report)
+    linf = None
+    if kind != 0:
+        norms = s.error_norms(t)
+        linf = {"velocity_linf": norms[2], "velocity_l2": norms[1], "t": t}
+
+    # per-kernel-class timing (real steps, launch by launch) -> dominant class
+    prof = s.profile_step(t, reps=2)
+    t += 2 * dt
+    peak, peak_kind = measured_peaks()
+    classes = {k: v for k, v in prof.items() if k in SWEEPS}
+    dom = max(classes, key=lambda k: classes[k])
+    alg_bytes_launch = SWEEPS[dom] * elem * cells
+    avg_launch_ms = classes[dom] / LAUNCHES_PER_STEP[dom]
+    achieved = alg_bytes_launch / (avg_launch_ms / 1e3) / 1e9
+    traffic = None
+    tr_path = os.path.join(REPO, "profiles", f"traffic_{args.workload}_{args.precision}.json")
+    if os.path.exists(tr_path):
+        with open(tr_path) as f:
+            traffic = json.load(f).get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": round(avg_launch_ms, 4)}
+    step_ms = ms / args.steps
+    step_roofline = STEP_SWEEPS * elem * cells / (step_ms / 1e3) / 1e9
+
+    # end to end through the drop-in host call, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        names = ("u", "v", "w", "p")
+        host = {nm: torch.empty(s.shape(nm), dtype=torch.float64, pin_memory=True) for nm in names}
+        for nm in names:
+            host[nm].numpy()[...] = s.download(nm)
+        bi = sum(h.numel() * 8 for h in host.values())
+        import numpy as np
+
+        arrs = [host[nm].numpy() for nm in names]
+        s.timestep_host(t, *arrs)  # warm
+        t += dt
+        k_e2e = max(1, min(args.steps, 3))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(k_e2e):
+            s.timestep_host(t, *arrs)
+            t += dt
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        el = allreduce_max(el, world)
+        e2e = {"value": world * cells * k_e2e / el / 1e9, "unit": UNIT, "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": bi, "steps": k_e2e, "api": "mifgpu_timestep_host"}
+        del np
+
+    # FP64 comparison point on the same workload (fewer steps; FP64 is ALU-bound on GB300)
+    fp64 = None
+    if prec == mifgpu.MIXED and not args.no_fp64:
+        s.close()
+        torch.cuda.empty_cache()
+        s64 = mifgpu.Solver(n_global=n_global, size=size, origin=origin, Re=Re, dt=dt, periodic=periodic,
+                            precision=mifgpu.FP64, boundary_kind=kind, forcing=forcing)
+        s64.set_stream(stream.cuda_stream)
+        s64.set_exact_velocity(0, 0.0)
+        s64.set_exact_pressure(0.0)
+        n64 = max(1, min(args.steps, 3))
+        s64.run(0.0, 1)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        s64.run(dt, n64)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = a0.elapsed_time(a1) / n64
+        fp64 = {"ms_per_step": round(ms64, 3), "value": cells / (ms64 / 1e3) / 1e9,
+                "mixed_speedup": round(ms64 / step_ms, 2)}
+        s64.run((1 + n64) * dt, max(0, args.warmup + args.steps - 1 - n64))
+        if kind != 0:
+            t64 = (args.warmup + args.steps) * dt
+            fp64["velocity_linf"] = s64.error_norms(t64)[2]
+            fp64["t"] = t64
+        s64.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(workers=1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if prec == mifgpu.MIXED else "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "n_global": list(n_global), "cells": cells,
+                       "precision": args.precision, "periodic": list(periodic), "Re": Re, "dt": dt,
+                       "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (fields ~%.1f GB)" %
+                       (11 * elem * cells / 1e9)},
+            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "step_roofline": {"bytes_per_cell_step": STEP_SWEEPS * elem, "achieved_gbs": round(step_roofline, 1),
+                              "frac": round(step_roofline / peak, 4)},
+            "kernel_ms_per_step": {k: round(v, 4) for k, v in prof.items()},
+            "error": linf, "fp64": fp64, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    vals = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(workers=cores, n=65, steps=1)
+        if k >= args.warmup:
+            vals.append(r["value"])
+    el = time.perf_counter() - t0
+    value = statistics.median(vals) if vals else 0.0
+    n_global = WORKLOADS[args.workload][0]
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "n_global": list(n_global), "sample": "64^3 cells per core"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"64^3-cell manufactured cube, 1 step per core per bench step, {cores} "
+                                       f"independent replicas (wall {el:.1f}s)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cube512", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -155,6 +155,27 @@ int mifgpu_adjust_pressure(mifgpu_ctx *ctx, double t);
  * (src/Norms.cpp:11-118). Reductions in double. */
 int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]);
 
+/* Kernel classes of one projection step, for mifgpu_profile_step. */
+enum mifgpu_prof_class {
+  MIFGPU_PROF_STAGE = 0,      /* the three fused RK stage updates */
+  MIFGPU_PROF_BOUNDARY = 1,   /* Dirichlet faces + periodic copies of the velocity */
+  MIFGPU_PROF_DIVERGENCE = 2, /* Poisson right-hand side */
+  MIFGPU_PROF_X_FORWARD = 3,  /* line transforms: x forward */
+  MIFGPU_PROF_Y_FORWARD = 4,  /* y forward */
+  MIFGPU_PROF_Z_FUSED = 5,    /* z forward, eigenvalue division, z inverse */
+  MIFGPU_PROF_Y_INVERSE = 6,  /* y inverse */
+  MIFGPU_PROF_X_INVERSE = 7,  /* x inverse */
+  MIFGPU_PROF_PERIODIC = 8,   /* periodic refresh of phi */
+  MIFGPU_PROF_PROJECT = 9,    /* p += phi, u -= dt grad phi */
+  MIFGPU_PROF_CLASSES = 10
+};
+
+/* Runs `reps` projection steps from t_n launch by launch (not from the graph),
+ * timing every kernel class with CUDA events on the context's stream; writes
+ * the mean milliseconds per step of each class. The steps are real: the
+ * fields advance. No counterpart in the reference (instrumentation). */
+int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIFGPU_PROF_CLASSES]);
+
 /* Number of kernels this context has launched so far (for launch accounting). */
 int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out);
 

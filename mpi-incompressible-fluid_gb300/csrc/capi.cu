@@ -35,6 +35,7 @@ struct ImplBase {
   virtual int project(mifgpu_ctx *ctx, int set, double dt) = 0;
   virtual int adjust_pressure(mifgpu_ctx *ctx, double t) = 0;
   virtual int error_norms(mifgpu_ctx *ctx, double t, double out[9]) = 0;
+  virtual int profile_step(mifgpu_ctx *ctx, double t_n, int reps, double *ms) = 0;
   virtual void swap_sets() = 0;
   virtual size_t bytes() const = 0;
 };
@@ -143,6 +144,16 @@ struct Impl final : ImplBase {
   cudaGraphExec_t graph[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   long long graph_launches[3][2] = {{0, 0}, {0, 0}, {0, 0}};
   size_t total_bytes = 0;
+  // Per-kernel-class event marks of a profiled (non-graph) step.
+  std::vector<std::pair<int, cudaEvent_t>> *prof = nullptr;
+
+  void mark(int cls, cudaStream_t s) {
+    if (!prof) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    prof->push_back({cls, e});
+  }
 
   ~Impl() override {
     for (auto &gv : graph)
@@ -261,20 +272,27 @@ struct Impl final : ImplBase {
   void enqueue_pressure(mifgpu_ctx *ctx, cudaStream_t s, int set, double dt, bool nhn, int slot_new, int slot_old,
                         bool solve, long long *cnt) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    mark(MIFGPU_PROF_DIVERGENCE, s);
     launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
     if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
     if (!solve) return;
-    ps.solve(F.f[kPhi], s, cnt);
+    if (prof)
+      ps.solve(F.f[kPhi], s, cnt, [&](int q) { mark(MIFGPU_PROF_X_FORWARD + q, s); });
+    else
+      ps.solve(F.f[kPhi], s, cnt);
+    mark(MIFGPU_PROF_PERIODIC, s);
     launch_periodic_scalar<T>(g, F.f[kPhi], s, cnt);
   }
 
   void enqueue_bc(mifgpu_ctx *ctx, cudaStream_t s, int set, int t_slot, long long *cnt) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    mark(MIFGPU_PROF_BOUNDARY, s);
     launch_apply_bc<T>(g, vel, ctx->prm.boundary_kind, 0, tref(), t_slot, s, cnt);
   }
 
   void enqueue_project(cudaStream_t s, int set, double dt, long long *cnt) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    mark(MIFGPU_PROF_PROJECT, s);
     launch_project<T>(g, F.f[kP], F.f[kPhi], vel, dt, s, cnt);
   }
 
@@ -302,6 +320,7 @@ struct Impl final : ImplBase {
     const int sin_slot[3] = {4, 6, 8};
     for (int st = 0; st < 3; ++st) {
       StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing};
+      mark(MIFGPU_PROF_STAGE, s);
       launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt);
       enqueue_bc(ctx, s, out_set[st], 1 + st, cnt);
       enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt);
@@ -340,6 +359,30 @@ struct Impl final : ImplBase {
     }
     // The host copy of the slots may be a temporary: wait until it was consumed.
     CK(cudaStreamSynchronize(ctx->stream));
+    return MIFGPU_OK;
+  }
+
+  int profile_step(mifgpu_ctx *ctx, double t_n, int reps, double *ms) override {
+    double sl[kSlotSize];
+    projection_slot(t_n, g.dt, sl);
+    CK(cudaMemcpyAsync(slots, sl, sizeof(sl), cudaMemcpyHostToDevice, ctx->stream));
+    for (int c = 0; c < MIFGPU_PROF_CLASSES; ++c) ms[c] = 0.0;
+    for (int r = 0; r < reps; ++r) {
+      std::vector<std::pair<int, cudaEvent_t>> marks;
+      prof = &marks;
+      CK(cudaMemsetAsync(step_ctr, 0, sizeof(int), ctx->stream));
+      enqueue_step(ctx, ctx->stream, kVariantProjection, &ctx->launches);
+      mark(-1, ctx->stream);
+      prof = nullptr;
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      for (size_t q = 0; q + 1 < marks.size(); ++q) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, marks[q].second, marks[q + 1].second);
+        ms[marks[q].first] += t / reps;
+      }
+      for (auto &m : marks) cudaEventDestroy(m.second);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "profiled step");
+    }
     return MIFGPU_OK;
   }
 
@@ -604,6 +647,11 @@ int mifgpu_adjust_pressure(mifgpu_ctx *ctx, double t) {
 int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]) {
   if (!ctx || !out) return MIFGPU_EINVAL;
   return ctx->impl->error_norms(ctx, t, out);
+}
+
+int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIFGPU_PROF_CLASSES]) {
+  if (!ctx || !ms_out || reps < 1) return MIFGPU_EINVAL;
+  return ctx->impl->profile_step(ctx, t_n, reps, ms_out);
 }
 
 int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out) {

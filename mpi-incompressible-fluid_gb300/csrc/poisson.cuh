@@ -1,6 +1,7 @@
 // Host interface of the spectral Poisson solver (poisson.cu).
 #pragma once
 
+#include <functional>
 #include <string>
 
 #include "common.cuh"
@@ -33,7 +34,9 @@ struct PoissonSolver {
   int init(const Geometry &g, std::string &err);
   void release();
   // In place on the owner block of phi: rhs in, solution out (no periodic refresh).
-  int solve(T *phi, cudaStream_t stream, long long *launches);
+  // `mark`, when set, is called with the sweep id (0 x-forward, 1 y-forward,
+  // 2 z forward+eigen+inverse, 3 y-inverse, 4 x-inverse) before each launch.
+  int solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark = nullptr);
 };
 
 }  // namespace mifgpu

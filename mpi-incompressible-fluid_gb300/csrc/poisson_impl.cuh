@@ -356,7 +356,7 @@ static LineArgs<T> make_args(const Geometry &g, const AxisPlan<T> &ax, int d, T 
 }
 
 template <typename T>
-int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches) {
+int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark) {
   const Geometry &g = geo;
   // Inverse normalisations, src/PressureEquation.cpp:167,200,234:
   // (points - 1) * (periodic ? 1 : 2), applied as a product with the reciprocal.
@@ -381,11 +381,13 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches) {
       line_kernel<T, kModeFwdEigInv><<<grid, kThreads, ax.smem, stream>>>(a);
     if (launches) ++*launches;
   };
-  launch(0, kModeForward, 1.0);
-  launch(1, kModeForward, 1.0);
-  launch(2, kModeFwdEigInv, norm[2]);
-  launch(1, kModeInverse, norm[1]);
-  launch(0, kModeInverse, norm[0]);
+  const int seq_axis[5] = {0, 1, 2, 1, 0};
+  const int seq_mode[5] = {kModeForward, kModeForward, kModeFwdEigInv, kModeInverse, kModeInverse};
+  const double seq_scale[5] = {1.0, 1.0, norm[2], norm[1], norm[0]};
+  for (int q = 0; q < 5; ++q) {
+    if (mark) mark(q);
+    launch(seq_axis[q], seq_mode[q], seq_scale[q]);
+  }
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -2;
 }
 

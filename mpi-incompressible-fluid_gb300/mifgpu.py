@@ -32,8 +32,11 @@ EXPORTED = [
     "mifgpu_field_extent", "mifgpu_upload", "mifgpu_download", "mifgpu_set_exact_velocity",
     "mifgpu_set_exact_pressure", "mifgpu_timestep", "mifgpu_run", "mifgpu_timestep_host", "mifgpu_timestep_nhn",
     "mifgpu_timestep_velocity", "mifgpu_apply_bc", "mifgpu_solve_pressure", "mifgpu_divergence", "mifgpu_project",
-    "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_launch_count", "mifgpu_device_bytes",
+    "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_profile_step", "mifgpu_launch_count",
+    "mifgpu_device_bytes",
 ]
+PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
+                   "x_inverse", "periodic", "project"]
 
 
 class MifGpuError(RuntimeError):
@@ -87,6 +90,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_project": [vp, i, d],
         "mifgpu_adjust_pressure": [vp, d],
         "mifgpu_error_norms": [vp, d, dp],
+        "mifgpu_profile_step": [vp, d, i, dp],
         "mifgpu_launch_count": [vp, dp],
         "mifgpu_device_bytes": [vp, dp],
     }
@@ -229,6 +233,12 @@ class Solver:
 
     def adjust_pressure(self, t: float) -> None:
         self._check(self.lib.mifgpu_adjust_pressure(self.h, t), "adjust_pressure")
+
+    def profile_step(self, t_n: float, reps: int = 1) -> dict:
+        """Mean ms per step of each kernel class (runs `reps` real steps)."""
+        out = np.zeros(len(PROFILE_CLASSES))
+        self._check(self.lib.mifgpu_profile_step(self.h, t_n, reps, out.ctypes.data), "profile_step")
+        return dict(zip(PROFILE_CLASSES, out.tolist()))
 
     def error_norms(self, t: float) -> np.ndarray:
         out = np.zeros(9)
