@@ -59,13 +59,39 @@ static void fft_rec(const cplx *x, long s, cplx *y, int n, const cplx *tw, long 
   }
 }
 
+/* Twiddle tables are cached per (length, sign): a solve transforms thousands
+ * of lines of the same length. Not thread-safe (the oracle is single-threaded;
+ * parallel CPU runs use separate processes). */
+enum { kCacheSlots = 8 };
+static struct {
+  int L, sign;
+  cplx *tw;
+} tw_cache[kCacheSlots];
+static int tw_next;
+static cplx *tmp_buf;
+static long tmp_cap;
+
+static const cplx *twiddles(int L, int sign) {
+  for (int q = 0; q < kCacheSlots; ++q)
+    if (tw_cache[q].tw && tw_cache[q].L == L && tw_cache[q].sign == sign) return tw_cache[q].tw;
+  const int q = tw_next;
+  tw_next = (tw_next + 1) % kCacheSlots;
+  free(tw_cache[q].tw);
+  tw_cache[q].tw = (cplx *)malloc(sizeof(cplx) * (size_t)L);
+  tw_cache[q].L = L;
+  tw_cache[q].sign = sign;
+  for (long e = 0; e < L; ++e) tw_cache[q].tw[e] = unit_root(e, L, sign);
+  return tw_cache[q].tw;
+}
+
 static void fft(const cplx *x, cplx *y, int L, int sign) {
-  cplx *tw = (cplx *)malloc(sizeof(cplx) * (size_t)L);
-  cplx *tmp = (cplx *)malloc(sizeof(cplx) * (size_t)L);
-  for (long e = 0; e < L; ++e) tw[e] = unit_root(e, L, sign);
-  fft_rec(x, 1, y, L, tw, L, tmp);
-  free(tw);
-  free(tmp);
+  const cplx *tw = twiddles(L, sign);
+  if (tmp_cap < L) {
+    free(tmp_buf);
+    tmp_buf = (cplx *)malloc(sizeof(cplx) * (size_t)L);
+    tmp_cap = L;
+  }
+  fft_rec(x, 1, y, L, tw, L, tmp_buf);
 }
 
 int oracle_r2r_1d(int n, int kind, const double *in, double *out) {
