@@ -49,11 +49,14 @@ WORKLOADS = {
     "channel512x256x512": ((513, 257, 513), (4 * 3.141592653589793, 2.0, 2 * 3.141592653589793), (0.0, 0.0, 0.0),
                            (True, False, True), 5000.0, 5e-4, 0, 0),
     "cube64": ((65, 65, 65), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0, 1e-4, 1, 2),
+    # profiling case: ~1.5 GB on the device, z lines still DCT-I of 513 points
+    "box256x256x512": ((257, 257, 513), (0.5, 0.5, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
+                       1e-4 * (64.0 / 512.0) ** 2, 1, 2),
 }
 
 # Algorithmic HBM sweeps (full-field reads + writes) per launch of each kernel
 # class; times the field bytes and the cell count give algorithmic bytes.
-SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 2.0, "y_forward": 2.0, "z_fused": 2.0,
+SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 4.0, "y_forward": 2.0, "z_fused": 2.0,
           "y_inverse": 2.0, "x_inverse": 2.0, "project": 9.0}
 LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3, "z_fused": 3, "y_inverse": 3,
                      "x_inverse": 3, "project": 3}

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -272,14 +273,18 @@ struct Impl final : ImplBase {
   void enqueue_pressure(mifgpu_ctx *ctx, cudaStream_t s, int set, double dt, bool nhn, int slot_new, int slot_old,
                         bool solve, long long *cnt) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
-    mark(MIFGPU_PROF_DIVERGENCE, s);
-    launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
-    if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
+    // The divergence is fused into the x-forward sweep unless the boundary
+    // flux of the non-homogeneous Neumann problem has to be added in between.
+    const bool fused = solve && !nhn;
+    if (!fused) {
+      mark(MIFGPU_PROF_DIVERGENCE, s);
+      launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
+      if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
+    }
     if (!solve) return;
-    if (prof)
-      ps.solve(F.f[kPhi], s, cnt, [&](int q) { mark(MIFGPU_PROF_X_FORWARD + q, s); });
-    else
-      ps.solve(F.f[kPhi], s, cnt);
+    std::function<void(int)> mk;
+    if (prof) mk = [&](int q) { mark(MIFGPU_PROF_X_FORWARD + q, s); };
+    ps.solve(F.f[kPhi], s, cnt, mk, fused ? vel : nullptr, dt);
     mark(MIFGPU_PROF_PERIODIC, s);
     launch_periodic_scalar<T>(g, F.f[kPhi], s, cnt);
   }

@@ -152,8 +152,10 @@ struct SmallDft<T2, 8> {
 };
 
 // One Stockham stage of radix R over P rows. Ns = product of earlier radices.
-template <typename T2, int R, int MAXE>
-__device__ __forceinline__ void fft_stage(T2 *s, int LS, int P, int L, int Ns, int sign, const T2 *tw) {
+// POW2: L, R and Ns are powers of two and the index arithmetic uses shifts
+// (lg_* are their base-2 logarithms); otherwise it divides.
+template <typename T2, int R, int MAXE, int SIGN, bool POW2>
+__device__ __forceinline__ void fft_stage(T2 *s, int LS, int P, int L, int Ns, const T2 *tw, int lg_nbf, int lg_ns) {
   constexpr int NB = MAXE / R;
   const int nbf = L / R;
   const int total = P * nbf;
@@ -163,13 +165,21 @@ __device__ __forceinline__ void fft_stage(T2 *s, int LS, int P, int L, int Ns, i
   for (int e = 0; e < NB; ++e) {
     const int b = threadIdx.x + e * blockDim.x;
     if (b < total) {
-      const int pp = b / nbf, j = b - pp * nbf;
-      const int k = j % Ns;
+      int pp, j, k;
+      if (POW2) {
+        pp = b >> lg_nbf;
+        j = b & (nbf - 1);
+        k = j & (Ns - 1);
+      } else {
+        pp = b / nbf;
+        j = b - pp * nbf;
+        k = j % Ns;
+      }
       const T2 *row = s + pp * LS;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         T2 x = row[j + q * nbf];
-        if (q > 0 && k > 0) x = cmul(x, twiddle(tw, q * k * twstep, sign));
+        if (q > 0 && k > 0) x = cmul(x, twiddle(tw, q * k * twstep, SIGN));
         v[e][q] = x;
       }
     }
@@ -179,11 +189,20 @@ __device__ __forceinline__ void fft_stage(T2 *s, int LS, int P, int L, int Ns, i
   for (int e = 0; e < NB; ++e) {
     const int b = threadIdx.x + e * blockDim.x;
     if (b < total) {
-      SmallDft<T2, R>::run(v[e], sign, tw, L);
-      const int pp = b / nbf, j = b - pp * nbf;
-      const int k = j % Ns;
+      SmallDft<T2, R>::run(v[e], SIGN, tw, L);
+      int pp, j, k, out0;
+      if (POW2) {
+        pp = b >> lg_nbf;
+        j = b & (nbf - 1);
+        k = j & (Ns - 1);
+        out0 = ((j >> lg_ns) << (lg_ns + __ffs(R) - 1)) + k;
+      } else {
+        pp = b / nbf;
+        j = b - pp * nbf;
+        k = j % Ns;
+        out0 = (j / Ns) * Ns * R + k;
+      }
       T2 *row = s + pp * LS;
-      const int out0 = (j / Ns) * Ns * R + k;
 #pragma unroll
       for (int q = 0; q < R; ++q) row[out0 + q * Ns] = v[e][q];
     }
@@ -229,24 +248,35 @@ struct FftFactors {
   int f[16];
 };
 
-template <typename T2, int MAXE>
-__device__ void fft_rows(T2 *s, int LS, int P, int L, const FftFactors &fac, int sign, const T2 *tw) {
-  int Ns = 1;
+template <typename T2, int MAXE, int SIGN, bool POW2>
+__device__ void fft_rows_t(T2 *s, int LS, int P, int L, const FftFactors &fac, const T2 *tw) {
+  int Ns = 1, lg_ns = 0;
   for (int q = 0; q < fac.n; ++q) {
     const int R = fac.f[q];
+    const int lg_nbf = POW2 ? (__ffs(L / R) - 1) : 0;
     switch (R) {
-      case 2: fft_stage<T2, 2, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 3: fft_stage<T2, 3, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 4: fft_stage<T2, 4, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 5: fft_stage<T2, 5, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 7: fft_stage<T2, 7, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 8: fft_stage<T2, 8, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 11: fft_stage<T2, 11, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      case 13: fft_stage<T2, 13, MAXE>(s, LS, P, L, Ns, sign, tw); break;
-      default: dft_direct<T2, MAXE>(s, LS, P, L, sign, tw); break;
+      case 2: fft_stage<T2, 2, MAXE, SIGN, POW2>(s, LS, P, L, Ns, tw, lg_nbf, lg_ns); break;
+      case 4: fft_stage<T2, 4, MAXE, SIGN, POW2>(s, LS, P, L, Ns, tw, lg_nbf, lg_ns); break;
+      case 8: fft_stage<T2, 8, MAXE, SIGN, POW2>(s, LS, P, L, Ns, tw, lg_nbf, lg_ns); break;
+      case 3: if (!POW2) fft_stage<T2, 3, MAXE, SIGN, false>(s, LS, P, L, Ns, tw, 0, 0); break;
+      case 5: if (!POW2) fft_stage<T2, 5, MAXE, SIGN, false>(s, LS, P, L, Ns, tw, 0, 0); break;
+      case 7: if (!POW2) fft_stage<T2, 7, MAXE, SIGN, false>(s, LS, P, L, Ns, tw, 0, 0); break;
+      case 11: if (!POW2) fft_stage<T2, 11, MAXE, SIGN, false>(s, LS, P, L, Ns, tw, 0, 0); break;
+      case 13: if (!POW2) fft_stage<T2, 13, MAXE, SIGN, false>(s, LS, P, L, Ns, tw, 0, 0); break;
+      default: if (!POW2) dft_direct<T2, MAXE>(s, LS, P, L, SIGN, tw); break;
     }
     Ns *= R;
+    if (POW2) lg_ns += __ffs(R) - 1;
   }
+}
+
+// All rows of the CTA; `pow2` (uniform) selects the shift-indexed stages.
+template <typename T2, int MAXE, int SIGN>
+__device__ __forceinline__ void fft_rows(T2 *s, int LS, int P, int L, const FftFactors &fac, const T2 *tw, bool pow2) {
+  if (pow2)
+    fft_rows_t<T2, MAXE, SIGN, true>(s, LS, P, L, fac, tw);
+  else
+    fft_rows_t<T2, MAXE, SIGN, false>(s, LS, P, L, fac, tw);
 }
 
 }  // namespace mifgpu

@@ -16,7 +16,8 @@ struct AxisPlan {
   int n = 0, L = 0;
   int nfac = 0;
   int fac[16] = {0};
-  int P = 1;
+  int P = 1, lg_lines = 1;
+  bool pow2 = false;
   bool line_fast = false;
   size_t smem = 0;
   typename Vec2<T>::type *tw = nullptr;
@@ -30,13 +31,17 @@ template <typename T>
 struct PoissonSolver {
   Geometry geo{};
   AxisPlan<T> axis[3];
+  T *eig = nullptr;  // 1/(lambda sum) on the owner block, x fastest; 0 at the zero mode
 
   int init(const Geometry &g, std::string &err);
   void release();
   // In place on the owner block of phi: rhs in, solution out (no periodic refresh).
   // `mark`, when set, is called with the sweep id (0 x-forward, 1 y-forward,
   // 2 z forward+eigen+inverse, 3 y-inverse, 4 x-inverse) before each launch.
-  int solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark = nullptr);
+  // When `vel` is given, the x-forward sweep computes the right-hand side
+  // div(vel)/dt itself and phi's previous contents are not read.
+  int solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark = nullptr,
+            T *const *vel = nullptr, double dt = 1.0);
 };
 
 }  // namespace mifgpu

@@ -48,6 +48,8 @@ struct MaxE<double> {
 
 enum { kModeForward = 0, kModeInverse = 1, kModeFwdEigInv = 2 };
 
+constexpr int kMaxLines = 128;  // lines per CTA (2 P), a power of two
+
 template <typename T>
 struct LineArgs {
   T *data;
@@ -55,61 +57,105 @@ struct LineArgs {
   int na, nb;             // owner points along the two other axes (a varies fastest)
   int n, L, kind;         // points per line, complex FFT length, 0 DCT-I / 1 real DFT
   FftFactors fac;
+  int pow2;               // L is a power of two (shift-indexed FFT stages)
   const typename Vec2<T>::type *tw;
-  int P;          // line pairs per CTA
-  int line_fast;  // 1: consecutive threads take consecutive lines (strided axes)
-  double scale;   // output multiplier (inverse normalisation), 1 otherwise
-  // kModeFwdEigInv only: eigenvalues of axes a, b and of the line axis
-  const double *lam_a, *lam_b, *lam_n;
+  int P, lg_lines;        // line pairs per CTA; log2(2P)
+  int line_fast;          // 1: consecutive threads take consecutive lines (strided axes)
+  double scale;           // output multiplier (inverse normalisation), 1 otherwise
+  // kModeFwdEigInv only: 1/(lambda_x + lambda_y + lambda_z) on the owner block,
+  // x fastest, computed in double at set-up, zero mode 0.
+  const T *eig;
+  // x-forward sweep fused with the right-hand side: when du is set the line
+  // values are div(u)/dt at the owner points (src/PressureEquation.cpp:59-61,
+  // include/VelocityDivergence.h:9-20) instead of data[].
+  const T *du, *dv, *dw;
+  long vsy, vsz;
+  T doh[3];
+  T inv_dt;
+};
+
+// Per-CTA line table: global offset of each line's first element (-1 past the
+// end) and its eigenvalue-table offset.
+struct LineTable {
+  long off[kMaxLines];
+  long eoff[kMaxLines];
 };
 
 template <typename T>
-__device__ __forceinline__ long line_offset(const LineArgs<T> &a, long gl) {
-  const long qa = gl % a.na, qb = gl / a.na;
-  return a.base + qa * a.sa + qb * a.sb;
+__device__ void fill_line_table(LineTable &t, const LineArgs<T> &a, long line0, long total) {
+  const int nl = 2 * a.P;
+  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+    const long gl = line0 + l;
+    if (gl < total) {
+      const long qa = gl % a.na, qb = gl / a.na;
+      t.off[l] = a.base + qa * a.sa + qb * a.sb;
+      t.eoff[l] = qa + (long)a.na * qb;  // (x, y) of a z line in the owner block
+    } else {
+      t.off[l] = -1;
+      t.eoff[l] = 0;
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ T line_value(const LineArgs<T> &a, long q) {
+  if (a.du) {
+    const T du = (__ldg(a.du + q + 1) - __ldg(a.du + q)) * a.doh[0];
+    const T dv = (__ldg(a.dv + q + a.vsy) - __ldg(a.dv + q)) * a.doh[1];
+    const T dw = (__ldg(a.dw + q + a.vsz) - __ldg(a.dw + q)) * a.doh[2];
+    return (du + dv + dw) * a.inv_dt;
+  }
+  return a.data[q];
+}
+
+template <typename T>
+__device__ __forceinline__ void put(T *row, const LineArgs<T> &a, int l, int m, T v) {
+  row[2 * m + (l & 1)] = v;
+  if (a.kind == 0 && m > 0 && m < a.n - 1) row[2 * (a.L - m) + (l & 1)] = v;
 }
 
 // Global -> shared: line l of the CTA is component (l & 1) of row (l >> 1).
 template <typename T, typename T2>
-__device__ void load_lines(T2 *s, int LS, const LineArgs<T> &a, long line0, long total) {
+__device__ void load_lines(T2 *s, int LS, const LineArgs<T> &a, const LineTable &t) {
   const int nl = 2 * a.P;
-  const int cnt = nl * a.n;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    int l, m;
-    if (a.line_fast) {
-      m = e / nl;
-      l = e - m * nl;
-    } else {
-      l = e / a.n;
-      m = e - l * a.n;
+  if (a.line_fast) {
+    const int cnt = nl * a.n;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int m = e >> a.lg_lines, l = e & (nl - 1);
+      const long off = t.off[l];
+      const T v = off >= 0 ? line_value(a, off + (long)m * a.se) : T(0);
+      put(reinterpret_cast<T *>(s + (l >> 1) * LS), a, l, m, v);
     }
-    const long gl = line0 + l;
-    T v = T(0);
-    if (gl < total) v = a.data[line_offset(a, gl) + (long)m * a.se];
-    T *row = reinterpret_cast<T *>(s + (l >> 1) * LS);
-    row[2 * m + (l & 1)] = v;
-    if (a.kind == 0 && m > 0 && m < a.n - 1) row[2 * (a.L - m) + (l & 1)] = v;
+  } else {
+    for (int l = 0; l < nl; ++l) {
+      const long off = t.off[l];
+      T *row = reinterpret_cast<T *>(s + (l >> 1) * LS);
+      for (int m = threadIdx.x; m < a.n; m += blockDim.x) put(row, a, l, m, off >= 0 ? line_value(a, off + m) : T(0));
+    }
   }
   __syncthreads();
 }
 
 template <typename T, typename T2>
-__device__ void store_lines(const T2 *s, int LS, const LineArgs<T> &a, long line0, long total, T scale) {
+__device__ void store_lines(const T2 *s, int LS, const LineArgs<T> &a, const LineTable &t, T scale) {
   const int nl = 2 * a.P;
-  const int cnt = nl * a.n;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    int l, m;
-    if (a.line_fast) {
-      m = e / nl;
-      l = e - m * nl;
-    } else {
-      l = e / a.n;
-      m = e - l * a.n;
+  if (a.line_fast) {
+    const int cnt = nl * a.n;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int m = e >> a.lg_lines, l = e & (nl - 1);
+      const long off = t.off[l];
+      if (off >= 0) {
+        const T *row = reinterpret_cast<const T *>(s + (l >> 1) * LS);
+        a.data[off + (long)m * a.se] = row[2 * m + (l & 1)] * scale;
+      }
     }
-    const long gl = line0 + l;
-    if (gl < total) {
+  } else {
+    for (int l = 0; l < nl; ++l) {
+      const long off = t.off[l];
+      if (off < 0) continue;
       const T *row = reinterpret_cast<const T *>(s + (l >> 1) * LS);
-      a.data[line_offset(a, gl) + (long)m * a.se] = row[2 * m + (l & 1)] * scale;
+      for (int m = threadIdx.x; m < a.n; m += blockDim.x) a.data[off + m] = row[2 * m + (l & 1)] * scale;
     }
   }
 }
@@ -120,20 +166,19 @@ template <typename T2>
 __device__ void split_halfcomplex(T2 *s, int LS, int P, int n) {
   using T = decltype(s[0].x);
   const int half = (n + 1) / 2;  // k in [1, half)
-  const int cnt = P * (half - 1);
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int pp = e / (half - 1);
-    const int k = 1 + e - pp * (half - 1);
+  for (int pp = 0; pp < P; ++pp) {
     T2 *row = s + pp * LS;
-    const T2 zk = row[k], zm = row[n - k];
-    const T h = T(0.5);
-    T2 lo, hi;
-    lo.x = (zk.x + zm.x) * h;   // Re A_k
-    lo.y = (zk.y + zm.y) * h;   // Re B_k
-    hi.x = (zk.y - zm.y) * h;   // Im A_k
-    hi.y = -(zk.x - zm.x) * h;  // Im B_k
-    row[k] = lo;
-    row[n - k] = hi;
+    for (int k = 1 + threadIdx.x; k < half; k += blockDim.x) {
+      const T2 zk = row[k], zm = row[n - k];
+      const T h = T(0.5);
+      T2 lo, hi;
+      lo.x = (zk.x + zm.x) * h;   // Re A_k
+      lo.y = (zk.y + zm.y) * h;   // Re B_k
+      hi.x = (zk.y - zm.y) * h;   // Im A_k
+      hi.y = -(zk.x - zm.x) * h;  // Im B_k
+      row[k] = lo;
+      row[n - k] = hi;
+    }
   }
   __syncthreads();
 }
@@ -142,47 +187,37 @@ __device__ void split_halfcomplex(T2 *s, int LS, int P, int n) {
 template <typename T2>
 __device__ void merge_halfcomplex(T2 *s, int LS, int P, int n) {
   const int half = (n + 1) / 2;
-  const int cnt = P * (half - 1);
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int pp = e / (half - 1);
-    const int k = 1 + e - pp * (half - 1);
+  for (int pp = 0; pp < P; ++pp) {
     T2 *row = s + pp * LS;
-    const T2 hk = row[k], hm = row[n - k];
-    T2 zk, zm;
-    zk.x = hk.x - hm.y;
-    zk.y = hm.x + hk.y;
-    zm.x = hk.x + hm.y;
-    zm.y = hk.y - hm.x;
-    row[k] = zk;
-    row[n - k] = zm;
+    for (int k = 1 + threadIdx.x; k < half; k += blockDim.x) {
+      const T2 hk = row[k], hm = row[n - k];
+      T2 zk, zm;
+      zk.x = hk.x - hm.y;
+      zk.y = hm.x + hk.y;
+      zm.x = hk.x + hm.y;
+      zm.y = hk.y - hm.x;
+      row[k] = zk;
+      row[n - k] = zm;
+    }
   }
   __syncthreads();
 }
 
-// Spectrum * 1/(lambda_a + lambda_b + lambda_n) in double, mode (0,0,0) := 0
+// Spectrum times the precomputed 1/(lambda_x + lambda_y + lambda_z)
 // (src/PressureSolverStructures.cpp:52-69, src/PressureEquation.cpp:157-163).
 template <typename T, typename T2>
-__device__ void apply_eigenvalues(T2 *s, int LS, const LineArgs<T> &a, long line0, long total) {
-  const int cnt = a.P * a.n;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int pp = e / a.n;
-    const int m = e - pp * a.n;
+__device__ void apply_eigenvalues(T2 *s, int LS, const LineArgs<T> &a, const LineTable &t) {
+  const long plane = (long)a.na * a.nb;
+  for (int pp = 0; pp < a.P; ++pp) {
     T2 *row = s + pp * LS;
-    T2 v = row[m];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const long gl = line0 + 2 * pp + c;
-      if (gl >= total) continue;
-      const long qa = gl % a.na, qb = gl / a.na;
-      const double lsum = a.lam_a[qa] + a.lam_b[qb] + a.lam_n[m];
-      T &val = c == 0 ? v.x : v.y;
-      if (qa == 0 && qb == 0 && m == 0)
-        val = T(0);
-      else
-        val = T((double)val * (1.0 / lsum));
+    const long ea = t.eoff[2 * pp], eb = t.eoff[2 * pp + 1];
+    for (int m = threadIdx.x; m < a.n; m += blockDim.x) {
+      T2 v = row[m];
+      v.x = v.x * __ldg(a.eig + ea + plane * m);
+      v.y = v.y * __ldg(a.eig + eb + plane * m);
+      row[m] = v;
+      if (a.kind == 0 && m > 0 && m < a.n - 1) row[a.L - m] = v;
     }
-    row[m] = v;
-    if (a.kind == 0 && m > 0 && m < a.n - 1) row[a.L - m] = v;
   }
   __syncthreads();
 }
@@ -191,25 +226,47 @@ template <typename T, int MODE>
 __global__ void __launch_bounds__(kThreads) line_kernel(LineArgs<T> a) {
   using T2 = typename Vec2<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ LineTable table;
   T2 *s = reinterpret_cast<T2 *>(smem_raw);
   constexpr int MAXE = MaxE<T>::v;
   const int LS = a.L + 1;
   const long total = (long)a.na * a.nb;
   const long line0 = (long)blockIdx.x * 2 * a.P;
+  const bool pow2 = a.pow2 != 0;
 
-  load_lines(s, LS, a, line0, total);
-  if (a.kind == 1 && MODE == kModeInverse) merge_halfcomplex(s, LS, a.P, a.n);
-  const int sign0 = (a.kind == 1 && MODE == kModeInverse) ? +1 : -1;
-  fft_rows<T2, MAXE>(s, LS, a.P, a.L, a.fac, sign0, a.tw);
+  fill_line_table(table, a, line0, total);
+  load_lines(s, LS, a, table);
+  if (MODE == kModeInverse && a.kind == 1) {
+    merge_halfcomplex(s, LS, a.P, a.n);
+    fft_rows<T2, MAXE, +1>(s, LS, a.P, a.L, a.fac, a.tw, pow2);
+  } else {
+    fft_rows<T2, MAXE, -1>(s, LS, a.P, a.L, a.fac, a.tw, pow2);
+  }
   if (MODE == kModeFwdEigInv) {
     if (a.kind == 1) split_halfcomplex(s, LS, a.P, a.n);
-    apply_eigenvalues(s, LS, a, line0, total);
-    if (a.kind == 1) merge_halfcomplex(s, LS, a.P, a.n);
-    fft_rows<T2, MAXE>(s, LS, a.P, a.L, a.fac, a.kind == 1 ? +1 : -1, a.tw);
+    apply_eigenvalues(s, LS, a, table);
+    if (a.kind == 1) {
+      merge_halfcomplex(s, LS, a.P, a.n);
+      fft_rows<T2, MAXE, +1>(s, LS, a.P, a.L, a.fac, a.tw, pow2);
+    } else {
+      fft_rows<T2, MAXE, -1>(s, LS, a.P, a.L, a.fac, a.tw, pow2);
+    }
   } else if (MODE == kModeForward && a.kind == 1) {
     split_halfcomplex(s, LS, a.P, a.n);
   }
-  store_lines(s, LS, a, line0, total, T(a.scale));
+  store_lines(s, LS, a, table, T(a.scale));
+}
+
+// Inverse eigenvalue sums on the owner block (x fastest), in double, as the
+// reference tabulates them once (src/PressureSolverStructures.cpp:52-69).
+template <typename T>
+__global__ void eigen_table_kernel(T *eig, const double *lx, const double *ly, const double *lz, int nx, int ny,
+                                   int nz) {
+  const long n = (long)nx * ny * nz;
+  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(id % nx), j = (int)((id / nx) % ny), k = (int)(id / ((long)nx * ny));
+    eig[id] = (i == 0 && j == 0 && k == 0) ? T(0) : T(1.0 / (lx[i] + ly[j] + lz[k]));
+  }
 }
 
 int smallest_radix(int L) {
@@ -260,9 +317,17 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
   P = (int)(capacity / L);
   const long max_pairs = (line_count + 1) / 2;
   if (P > max_pairs) P = (int)std::max<long>(1, max_pairs);
+  if (P > kMaxLines / 2) P = kMaxLines / 2;
   const size_t row_bytes = sizeof(typename Vec2<T>::type) * (size_t)(L + 1);
   const size_t smem_cap = 96 * 1024;
   while (P > 1 && row_bytes * P > smem_cap) --P;
+  while (P & (P - 1)) --P;  // a power of two: line indices split with shifts
+  lg_lines = 0;
+  while ((1 << lg_lines) < 2 * P) ++lg_lines;
+  pow2 = (L & (L - 1)) == 0;
+  if (pow2)
+    for (int q = 0; q < nfac; ++q)
+      if (fac[q] & (fac[q] - 1)) pow2 = false;
   smem = row_bytes * P;
 
   // Twiddles exp(-2 pi i e / L) in long double, rounded once.
@@ -313,6 +378,18 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
     if (rc) return rc;
     smem_max = std::max(smem_max, axis[d].smem);
   }
+  // 1/(lambda_x + lambda_y + lambda_z) on the owner block, in double once.
+  const size_t ne = (size_t)g.np[0] * g.np[1] * g.np[2];
+  if (cudaMalloc(&eig, sizeof(T) * ne) != cudaSuccess) {
+    err = "cudaMalloc of the eigenvalue table failed";
+    return -2;
+  }
+  eigen_table_kernel<T><<<1024, 256>>>(eig, axis[0].lam_dev, axis[1].lam_dev, axis[2].lam_dev, g.np[0], g.np[1],
+                                       g.np[2]);
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    err = "eigenvalue table kernel failed";
+    return -2;
+  }
   // The limit is a property of the kernel function, shared by all three axes.
   for (int mode = 0; mode < 3; ++mode) {
     const void *fn = mode == 0   ? (const void *)line_kernel<T, kModeForward>
@@ -329,6 +406,8 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
 template <typename T>
 void PoissonSolver<T>::release() {
   for (auto &a : axis) a.release();
+  if (eig) cudaFree(eig);
+  eig = nullptr;
 }
 
 template <typename T>
@@ -348,15 +427,18 @@ static LineArgs<T> make_args(const Geometry &g, const AxisPlan<T> &ax, int d, T 
   a.kind = ax.kind;
   a.fac.n = ax.nfac;
   for (int q = 0; q < ax.nfac; ++q) a.fac.f[q] = ax.fac[q];
+  a.pow2 = ax.pow2 ? 1 : 0;
   a.tw = ax.tw;
   a.P = ax.P;
+  a.lg_lines = ax.lg_lines;
   a.line_fast = ax.line_fast ? 1 : 0;
   a.scale = 1.0;
   return a;
 }
 
 template <typename T>
-int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark) {
+int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark,
+                            T *const *vel, double dt) {
   const Geometry &g = geo;
   // Inverse normalisations, src/PressureEquation.cpp:167,200,234:
   // (points - 1) * (periodic ? 1 : 2), applied as a product with the reciprocal.
@@ -366,11 +448,16 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
     const AxisPlan<T> &ax = axis[d];
     LineArgs<T> a = make_args(g, ax, d, phi);
     a.scale = scale;
-    if (mode == kModeFwdEigInv) {
-      a.lam_a = axis[0].lam_dev;  // the z sweep's other axes are x (fast) and y
-      a.lam_b = axis[1].lam_dev;
-      a.lam_n = axis[2].lam_dev;
+    if (d == 0 && mode == kModeForward && vel) {
+      a.du = vel[0];
+      a.dv = vel[1];
+      a.dw = vel[2];
+      a.vsy = g.sy();
+      a.vsz = g.sz();
+      for (int q = 0; q < 3; ++q) a.doh[q] = T(g.oh[q]);
+      a.inv_dt = T(1.0 / dt);
     }
+    if (mode == kModeFwdEigInv) a.eig = eig;  // the z sweep's other axes are x (fast) and y
     const long total = (long)a.na * a.nb;
     const unsigned grid = (unsigned)((total + 2 * ax.P - 1) / (2 * ax.P));
     if (mode == kModeForward)
