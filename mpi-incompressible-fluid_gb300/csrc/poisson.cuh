@@ -17,6 +17,9 @@ struct AxisPlan {
   int nfac = 0;
   int fac[16] = {0};
   int P = 1, lg_lines = 1;
+  // register-resident path (float, power-of-two L): L = reg_n1 * reg_n2, 0 if unused
+  int reg_n1 = 0, reg_n2 = 0, reg_P = 0, reg_lg = 0;
+  size_t reg_smem = 0;
   bool pow2 = false;
   bool line_fast = false;
   size_t smem = 0;

@@ -24,10 +24,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "fft.cuh"
 #include "poisson.cuh"
+#include "regfft.cuh"
 
 namespace mifgpu {
 
@@ -207,14 +209,13 @@ __device__ void merge_halfcomplex(T2 *s, int LS, int P, int n) {
 // (src/PressureSolverStructures.cpp:52-69, src/PressureEquation.cpp:157-163).
 template <typename T, typename T2>
 __device__ void apply_eigenvalues(T2 *s, int LS, const LineArgs<T> &a, const LineTable &t) {
-  const long plane = (long)a.na * a.nb;
   for (int pp = 0; pp < a.P; ++pp) {
     T2 *row = s + pp * LS;
-    const long ea = t.eoff[2 * pp], eb = t.eoff[2 * pp + 1];
+    const long ea = t.eoff[2 * pp] * a.n, eb = t.eoff[2 * pp + 1] * a.n;
     for (int m = threadIdx.x; m < a.n; m += blockDim.x) {
       T2 v = row[m];
-      v.x = v.x * __ldg(a.eig + ea + plane * m);
-      v.y = v.y * __ldg(a.eig + eb + plane * m);
+      v.x = v.x * __ldg(a.eig + ea + m);
+      v.y = v.y * __ldg(a.eig + eb + m);
       row[m] = v;
       if (a.kind == 0 && m > 0 && m < a.n - 1) row[a.L - m] = v;
     }
@@ -257,15 +258,187 @@ __global__ void __launch_bounds__(kThreads) line_kernel(LineArgs<T> a) {
   store_lines(s, LS, a, table, T(a.scale));
 }
 
-// Inverse eigenvalue sums on the owner block (x fastest), in double, as the
-// reference tabulates them once (src/PressureSolverStructures.cpp:52-69).
+// Inverse eigenvalue sums on the owner block, z fastest then x then y (the
+// reference's z-pencil order), in double, as the reference tabulates them
+// once (src/PressureSolverStructures.cpp:52-69). Zero mode: 0.
 template <typename T>
 __global__ void eigen_table_kernel(T *eig, const double *lx, const double *ly, const double *lz, int nx, int ny,
                                    int nz) {
   const long n = (long)nx * ny * nz;
   for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(id % nx), j = (int)((id / nx) % ny), k = (int)(id / ((long)nx * ny));
+    const int k = (int)(id % nz), i = (int)((id / nz) % nx), j = (int)(id / ((long)nz * nx));
     eig[id] = (i == 0 && j == 0 && k == 0) ? T(0) : T(1.0 / (lx[i] + ly[j] + lz[k]));
+  }
+}
+
+// ---- register-resident variant for power-of-two lengths (regfft.cuh) ----
+
+// Asynchronous 4-byte global -> shared copy (no register staging, many in flight).
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
+
+// The pair (a[m], b[m]) of the CTA's line pair: from the shared-memory row
+// (strided axes) or straight from global memory (contiguous x lines).
+template <typename T>
+struct PairSource {
+  const typename Vec2<T>::type *row;  // strided axes: staged row
+  const LineArgs<T> *a;               // x lines: global rows
+  long off_a, off_b;
+  __device__ __forceinline__ typename Vec2<T>::type operator()(int m) const {
+    if (row) return row[m];
+    typename Vec2<T>::type v;
+    v.x = off_a >= 0 ? line_value(*a, off_a + m) : T(0);
+    v.y = off_b >= 0 ? line_value(*a, off_b + m) : T(0);
+    return v;
+  }
+};
+
+// Element m of the first FFT's input: the even extension (DCT-I), the plain
+// pair (R2HC), or Z_k = A_k + i B_k rebuilt from two half-complex lines (HC2R).
+template <typename T2, typename Src>
+__device__ __forceinline__ T2 reg_input(const Src &src, int m, int n, int L, int kind, bool hc2r) {
+  if (kind == 0) return src(m < n ? m : L - m);
+  if (!hc2r || m == 0 || 2 * m == L) return src(m);
+  T2 z;
+  if (2 * m < L) {
+    const T2 hk = src(m), hm = src(L - m);
+    z.x = hk.x - hm.y;
+    z.y = hm.x + hk.y;
+  } else {
+    const T2 hk = src(L - m), hm = src(m);
+    z.x = hk.x + hm.y;
+    z.y = hk.y - hm.x;
+  }
+  return z;
+}
+
+// Element m of the z sweep's second FFT: the spectrum X (natural order in
+// row) times the inverse eigenvalues of the pair's two lines.
+template <typename T, typename T2>
+__device__ __forceinline__ T2 reg_eig_input(const T2 *row, int m, int n, int L, int kind, const T *ea, const T *eb) {
+  if (kind == 0) {
+    const int mm = m < n ? m : L - m;
+    T2 v = row[mm];
+    v.x = v.x * __ldg(ea + mm);
+    v.y = v.y * __ldg(eb + mm);
+    return v;
+  }
+  const T2 xm = row[m], xn = row[(L - m) & (L - 1)];
+  const T h = T(0.5);
+  const T ga = __ldg(ea + m) * h, gb = __ldg(eb + m) * h;
+  // eig_a A_m + i eig_b B_m with A = (X_m + conj X_-m)/2, B = (X_m - conj X_-m)/(2i)
+  T2 z;
+  z.x = ga * (xm.x + xn.x) + gb * (xm.x - xn.x);
+  z.y = ga * (xm.y - xn.y) + gb * (xm.y + xn.y);
+  return z;
+}
+
+// Two register passes of one length-L FFT for the pair owned by this thread
+// group; inputs come from `in(m)`, the result X[k] lands in row[k].
+template <typename T, int N1, int N2, int SIGN, typename Input>
+__device__ __forceinline__ void reg_fft_pair(typename Vec2<T>::type *row, int t, const typename Vec2<T>::type *tw,
+                                             Input in) {
+  using T2 = typename Vec2<T>::type;
+  constexpr int L = N1 * N2;
+  T2 x[N1];
+#pragma unroll
+  for (int n1 = 0; n1 < N1; ++n1) x[n1] = in(n1 * N2 + t);
+  RegDft<T2, N1, SIGN>::run(x);
+#pragma unroll
+  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], twiddle(tw, (t * k1) & (L - 1), SIGN));
+  __syncthreads();  // every thread has read its inputs from the row
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1) row[k1 * (N2 + 1) + t] = x[k1];
+  __syncthreads();
+  constexpr int R = N1 / N2;  // columns per thread
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int k1 = t + r * N2;
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) x[r * N2 + n2] = row[k1 * (N2 + 1) + n2];
+    RegDft<T2, N2, SIGN>::run(x + r * N2);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) row[t + r * N2 + N1 * k2] = x[r * N2 + k2];
+  __syncthreads();
+}
+
+template <typename T, int N1, int N2, int MODE>
+__global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
+  using T2 = typename Vec2<T>::type;
+  constexpr int L = N1 * N2;
+  constexpr int ROW = RegShape<N1, N2>::ROW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ LineTable table;
+  T2 *s = reinterpret_cast<T2 *>(smem_raw);
+  const long total = (long)a.na * a.nb;
+  const long line0 = (long)blockIdx.x * 2 * a.P;
+  const int pp = threadIdx.x / N2, t = threadIdx.x % N2;
+  T2 *row = s + pp * ROW;
+  const int n = a.n, kind = a.kind;
+  const int nl = 2 * a.P;
+
+  fill_line_table(table, a, line0, total);
+  if (a.line_fast) {
+    // Strided lines: stage the 2P x n tile asynchronously, consecutive threads
+    // on consecutive lines (consecutive addresses).
+    const int cnt = nl * n;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int m = e >> a.lg_lines, l = e & (nl - 1);
+      T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW + m) + (l & 1);
+      const long off = table.off[l];
+      if (off >= 0)
+        cp_async4(dst, a.data + off + (long)m * a.se);
+      else
+        *dst = T(0);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  PairSource<T> src{a.line_fast ? row : nullptr, &a, table.off[2 * pp], table.off[2 * pp + 1]};
+  const bool hc2r = MODE == kModeInverse && kind == 1;
+  if (hc2r)
+    reg_fft_pair<T, N1, N2, +1>(row, t, a.tw, [&](int m) { return reg_input<T2>(src, m, n, L, kind, true); });
+  else
+    reg_fft_pair<T, N1, N2, -1>(row, t, a.tw, [&](int m) { return reg_input<T2>(src, m, n, L, kind, false); });
+  if (MODE == kModeFwdEigInv) {
+    const T *ea = a.eig + table.eoff[2 * pp] * n, *eb = a.eig + table.eoff[2 * pp + 1] * n;
+    if (kind == 1)
+      reg_fft_pair<T, N1, N2, +1>(row, t, a.tw, [&](int m) { return reg_eig_input(row, m, n, L, kind, ea, eb); });
+    else
+      reg_fft_pair<T, N1, N2, -1>(row, t, a.tw, [&](int m) { return reg_eig_input(row, m, n, L, kind, ea, eb); });
+  }
+  // store: row[m] holds X[m]; the forward real DFT splits the pair into
+  // FFTW's half-complex order on the way out.
+  const T scale = T(a.scale);
+  const bool split = MODE == kModeForward && kind == 1;
+  auto value = [&](const T2 *r, int m, int comp) -> T {
+    if (!split) return (comp ? r[m].y : r[m].x) * scale;
+    const T2 xm = r[m], xn = r[(L - m) & (L - 1)];
+    const T h = T(0.5);
+    if (2 * m <= L) return comp ? (xm.y + xn.y) * h : (xm.x + xn.x) * h;
+    return comp ? (xm.x - xn.x) * h : (xn.y - xm.y) * h;
+  };
+  if (a.line_fast) {
+    const int cnt = nl * n;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int m = e >> a.lg_lines, l = e & (nl - 1);
+      const long off = table.off[l];
+      if (off >= 0) a.data[off + (long)m * a.se] = value(s + (l >> 1) * ROW, m, l & 1);
+    }
+  } else {
+    for (int l = 0; l < nl; ++l) {
+      const long off = table.off[l];
+      if (off < 0) continue;
+      const T2 *r = s + (l >> 1) * ROW;
+      for (int m = threadIdx.x; m < n; m += blockDim.x) a.data[off + m] = value(r, m, l & 1);
+    }
   }
 }
 
@@ -279,6 +452,33 @@ int smallest_radix(int L) {
 }  // namespace
 
 // ---- host side ----
+
+// (N1, N2) instantiations of the register path and their launch.
+template <typename T>
+struct RegKernels {
+  static const void *get(int n1, int n2, int mode) {
+#define MIFGPU_REG_CASE(A, B)                                                        \
+  if (n1 == A && n2 == B)                                                            \
+    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward> \
+           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse> \
+                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv>;
+    MIFGPU_REG_CASE(8, 8)
+    MIFGPU_REG_CASE(16, 8)
+    MIFGPU_REG_CASE(16, 16)
+    MIFGPU_REG_CASE(32, 16)
+    MIFGPU_REG_CASE(32, 32)
+#undef MIFGPU_REG_CASE
+    return nullptr;
+  }
+};
+
+template <typename T>
+static void launch_reg(int n1, int n2, int mode, unsigned grid, size_t smem, cudaStream_t stream, LineArgs<T> a) {
+  const void *fn = RegKernels<T>::get(n1, n2, mode);
+  void *args[] = {&a};
+  cudaLaunchKernel(fn, dim3(grid), dim3(kThreads), args, smem, stream);
+}
+
 
 template <typename T>
 int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fast_, std::string &err) {
@@ -329,6 +529,18 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
     for (int q = 0; q < nfac; ++q)
       if (fac[q] & (fac[q] - 1)) pow2 = false;
   smem = row_bytes * P;
+  // Register-resident path (regfft.cuh): float, power-of-two L in [64, 1024].
+  reg_n1 = reg_n2 = 0;
+  if (std::is_same<T, float>::value && (L & (L - 1)) == 0 && L >= 64 && L <= 1024) {
+    int lg = 0;
+    while ((1 << lg) < L) ++lg;
+    reg_n1 = 1 << ((lg + 1) / 2);
+    reg_n2 = L / reg_n1;
+    reg_P = kThreads / reg_n2;
+    reg_lg = 0;
+    while ((1 << reg_lg) < 2 * reg_P) ++reg_lg;
+    reg_smem = sizeof(typename Vec2<T>::type) * (size_t)reg_P * (size_t)(reg_n1 * (reg_n2 + 1) + 1);
+  }
 
   // Twiddles exp(-2 pi i e / L) in long double, rounded once.
   std::vector<typename Vec2<T>::type> hw(L);
@@ -389,6 +601,17 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
   if (cudaDeviceSynchronize() != cudaSuccess) {
     err = "eigenvalue table kernel failed";
     return -2;
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (!axis[d].reg_n1) continue;
+    for (int mode = 0; mode < 3; ++mode) {
+      const void *fn = RegKernels<T>::get(axis[d].reg_n1, axis[d].reg_n2, mode);
+      if (!fn || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis[d].reg_smem) !=
+                     cudaSuccess) {
+        err = "register-path kernel set-up failed";
+        return -2;
+      }
+    }
   }
   // The limit is a property of the kernel function, shared by all three axes.
   for (int mode = 0; mode < 3; ++mode) {
@@ -459,6 +682,14 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
     }
     if (mode == kModeFwdEigInv) a.eig = eig;  // the z sweep's other axes are x (fast) and y
     const long total = (long)a.na * a.nb;
+    if (ax.reg_n1) {
+      a.P = ax.reg_P;
+      a.lg_lines = ax.reg_lg;
+      const unsigned grid = (unsigned)((total + 2 * a.P - 1) / (2 * a.P));
+      launch_reg<T>(ax.reg_n1, ax.reg_n2, mode, grid, ax.reg_smem, stream, a);
+      if (launches) ++*launches;
+      return;
+    }
     const unsigned grid = (unsigned)((total + 2 * ax.P - 1) / (2 * ax.P));
     if (mode == kModeForward)
       line_kernel<T, kModeForward><<<grid, kThreads, ax.smem, stream>>>(a);

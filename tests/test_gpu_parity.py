@@ -196,3 +196,28 @@ def test_poisson_solution_satisfies_discrete_laplacian(mifgpu_lib, cuda_device):
         resid = lap - rhs
         # the residual is the removed constant mode: constant everywhere
         assert np.abs(resid - resid.mean()).max() <= 1e-9 * np.abs(rhs).max()
+
+
+@pytest.mark.parametrize("shape,periodic", [
+    ((33, 65, 129), (False, False, False)),   # DCT-I lengths 64, 128, 256 (register path)
+    ((257, 17, 33), (False, False, False)),   # 512
+    ((513, 9, 17), (False, False, False)),    # 1024
+    ((65, 129, 33), (True, True, True)),      # real DFT lengths 64, 128, 32 (32: shared-memory path)
+    ((257, 65, 513), (True, False, True)),    # channel-like: 256 / DCT 128 / 512
+    ((17, 513, 9), (False, False, False)),    # 1024 along the strided y axis
+])
+def test_mixed_poisson_matches_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, periodic):
+    """Mixed-precision Poisson solve (register FFT for power-of-two lengths)
+    against the FP64 oracle on a random right-hand side."""
+    O = oracle_lib
+    case = O.Case(n_global=shape, size=(1.0, 0.7, 1.3), periodic=periodic, dt=1.0)
+    o = O.OracleSolver(case)
+    rng = np.random.default_rng(sum(shape))
+    st = {c: rng.standard_normal(o.shape(c)) for c in ("u", "v", "w")}
+    o.load_state(st)
+    o.solve_pressure(0, 0.5)
+    g = make_solver(mifgpu_lib, dict(n_global=shape, size=(1.0, 0.7, 1.3), periodic=periodic, dt=1.0), precision=1)
+    g.load_state(st)
+    g.solve_pressure(0, 0.5)
+    want = o.get("phi")
+    assert rel_err(g.download("phi"), want) <= 2e-5
