@@ -315,40 +315,57 @@ __device__ __forceinline__ T2 reg_input(const Src &src, int m, int n, int L, int
   return z;
 }
 
-// Element m of the z sweep's second FFT: the spectrum X (natural order in
-// row) times the inverse eigenvalues of the pair's two lines.
-template <typename T, typename T2>
-__device__ __forceinline__ T2 reg_eig_input(const T2 *row, int m, int n, int L, int kind, const T *ea, const T *eb) {
-  if (kind == 0) {
-    const int mm = m < n ? m : L - m;
-    T2 v = row[mm];
-    v.x = v.x * __ldg(ea + mm);
-    v.y = v.y * __ldg(eb + mm);
-    return v;
+// The z sweep's eigenvalue product on the spectrum X of the pair (natural
+// order in row), in place, by the N2 threads of the pair: DCT-I scales each
+// line's real spectrum; the real DFT forms eig_a A_m + i eig_b B_m with
+// A = (X_m + conj X_-m)/2, B = (X_m - conj X_-m)/(2i), pairwise for (m, L-m).
+template <typename T, int L, int KIND>
+__device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, int stride, int n, const T *ea,
+                                            const T *eb) {
+  using T2 = typename Vec2<T>::type;
+  if (KIND == 0) {
+    for (int m = t; m < n; m += stride) {
+      T2 v = row[m];
+      v.x = v.x * __ldg(ea + m);
+      v.y = v.y * __ldg(eb + m);
+      row[m] = v;
+    }
+    return;
   }
-  const T2 xm = row[m], xn = row[(L - m) & (L - 1)];
   const T h = T(0.5);
-  const T ga = __ldg(ea + m) * h, gb = __ldg(eb + m) * h;
-  // eig_a A_m + i eig_b B_m with A = (X_m + conj X_-m)/2, B = (X_m - conj X_-m)/(2i)
-  T2 z;
-  z.x = ga * (xm.x + xn.x) + gb * (xm.x - xn.x);
-  z.y = ga * (xm.y - xn.y) + gb * (xm.y + xn.y);
-  return z;
+  for (int m = t; 2 * m <= L; m += stride) {
+    const int mn = (L - m) & (L - 1);
+    const T2 xm = row[m], xn = row[mn];
+    T2 zm, zn;
+    {
+      const T ga = __ldg(ea + m) * h, gb = __ldg(eb + m) * h;
+      zm.x = ga * (xm.x + xn.x) + gb * (xm.x - xn.x);
+      zm.y = ga * (xm.y - xn.y) + gb * (xm.y + xn.y);
+    }
+    {
+      const T ga = __ldg(ea + mn) * h, gb = __ldg(eb + mn) * h;
+      zn.x = ga * (xn.x + xm.x) + gb * (xn.x - xm.x);
+      zn.y = ga * (xn.y - xm.y) + gb * (xn.y + xm.y);
+    }
+    row[m] = zm;
+    if (mn != m) row[mn] = zn;
+  }
 }
 
-// Two register passes of one length-L FFT for the pair owned by this thread
-// group; inputs come from `in(m)`, the result X[k] lands in row[k].
-template <typename T, int N1, int N2, int SIGN, typename Input>
-__device__ __forceinline__ void reg_fft_pair(typename Vec2<T>::type *row, int t, const typename Vec2<T>::type *tw,
-                                             Input in) {
+// One length-L forward FFT (exponent sign -1) of the pair owned by this
+// thread group, in two register passes; x holds the thread's inputs
+// x[n1] = z[n1*N2 + t] and the result X[k] lands in row[k], conjugated when
+// conj_out is set. (A sign +1 transform is conj(FFT(conj(z))): callers
+// conjugate the input and set conj_out, so only one copy of this code exists
+// per kernel.)
+template <typename T, int N1, int N2>
+__device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], typename Vec2<T>::type *row, int t,
+                                             const typename Vec2<T>::type *tw, bool conj_out) {
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
-  T2 x[N1];
+  RegDft<T2, N1, -1>::run(x);
 #pragma unroll
-  for (int n1 = 0; n1 < N1; ++n1) x[n1] = in(n1 * N2 + t);
-  RegDft<T2, N1, SIGN>::run(x);
-#pragma unroll
-  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], twiddle(tw, (t * k1) & (L - 1), SIGN));
+  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], tw[(t * k1) & (L - 1)]);
   __syncthreads();  // every thread has read its inputs from the row
 #pragma unroll
   for (int k1 = 0; k1 < N1; ++k1) row[k1 * (N2 + 1) + t] = x[k1];
@@ -359,17 +376,22 @@ __device__ __forceinline__ void reg_fft_pair(typename Vec2<T>::type *row, int t,
     const int k1 = t + r * N2;
 #pragma unroll
     for (int n2 = 0; n2 < N2; ++n2) x[r * N2 + n2] = row[k1 * (N2 + 1) + n2];
-    RegDft<T2, N2, SIGN>::run(x + r * N2);
+    RegDft<T2, N2, -1>::run(x + r * N2);
   }
   __syncthreads();
+  const T sy = conj_out ? T(-1) : T(1);
 #pragma unroll
   for (int r = 0; r < R; ++r)
 #pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) row[t + r * N2 + N1 * k2] = x[r * N2 + k2];
+    for (int k2 = 0; k2 < N2; ++k2) {
+      T2 v = x[r * N2 + k2];
+      v.y *= sy;
+      row[t + r * N2 + N1 * k2] = v;
+    }
   __syncthreads();
 }
 
-template <typename T, int N1, int N2, int MODE>
+template <typename T, int N1, int N2, int MODE, int KIND>
 __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
@@ -381,7 +403,7 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
   const long line0 = (long)blockIdx.x * 2 * a.P;
   const int pp = threadIdx.x / N2, t = threadIdx.x % N2;
   T2 *row = s + pp * ROW;
-  const int n = a.n, kind = a.kind;
+  const int n = a.n;
   const int nl = 2 * a.P;
 
   fill_line_table(table, a, line0, total);
@@ -402,22 +424,33 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
     __syncthreads();
   }
   PairSource<T> src{a.line_fast ? row : nullptr, &a, table.off[2 * pp], table.off[2 * pp + 1]};
-  const bool hc2r = MODE == kModeInverse && kind == 1;
-  if (hc2r)
-    reg_fft_pair<T, N1, N2, +1>(row, t, a.tw, [&](int m) { return reg_input<T2>(src, m, n, L, kind, true); });
-  else
-    reg_fft_pair<T, N1, N2, -1>(row, t, a.tw, [&](int m) { return reg_input<T2>(src, m, n, L, kind, false); });
-  if (MODE == kModeFwdEigInv) {
-    const T *ea = a.eig + table.eoff[2 * pp] * n, *eb = a.eig + table.eoff[2 * pp + 1] * n;
-    if (kind == 1)
-      reg_fft_pair<T, N1, N2, +1>(row, t, a.tw, [&](int m) { return reg_eig_input(row, m, n, L, kind, ea, eb); });
-    else
-      reg_fft_pair<T, N1, N2, -1>(row, t, a.tw, [&](int m) { return reg_eig_input(row, m, n, L, kind, ea, eb); });
+  const T *ea = nullptr, *eb = nullptr;
+  if (MODE == kModeFwdEigInv) ea = a.eig + table.eoff[2 * pp] * n, eb = a.eig + table.eoff[2 * pp + 1] * n;
+  constexpr int npass = MODE == kModeFwdEigInv ? 2 : 1;
+#pragma unroll 1
+  for (int pass = 0; pass < npass; ++pass) {
+    // pass 0: forward, or HC2R for the inverse real DFT; pass 1: eigenvalue
+    // product and the inverse transform of the z sweep
+    const bool plus = KIND == 1 && (MODE == kModeInverse || pass == 1);
+    if (pass == 1) {
+      reg_eig_row<T, L, KIND>(row, t, N2, n, ea, eb);
+      __syncthreads();
+    }
+    T2 x[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) {
+      const int m = n1 * N2 + t;
+      T2 v = pass == 0 ? reg_input<T2>(src, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
+                       : row[KIND == 0 ? (m < n ? m : L - m) : m];
+      if (plus) v.y = -v.y;
+      x[n1] = v;
+    }
+    reg_fft_core<T, N1, N2>(x, row, t, a.tw, plus);
   }
   // store: row[m] holds X[m]; the forward real DFT splits the pair into
   // FFTW's half-complex order on the way out.
   const T scale = T(a.scale);
-  const bool split = MODE == kModeForward && kind == 1;
+  const bool split = MODE == kModeForward && KIND == 1;
   auto value = [&](const T2 *r, int m, int comp) -> T {
     if (!split) return (comp ? r[m].y : r[m].x) * scale;
     const T2 xm = r[m], xn = r[(L - m) & (L - 1)];
@@ -453,28 +486,32 @@ int smallest_radix(int L) {
 
 // ---- host side ----
 
-// (N1, N2) instantiations of the register path and their launch.
+// (N1, N2) x mode x kind instantiations of the register path.
 template <typename T>
 struct RegKernels {
-  static const void *get(int n1, int n2, int mode) {
-#define MIFGPU_REG_CASE(A, B)                                                        \
-  if (n1 == A && n2 == B)                                                            \
-    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward> \
-           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse> \
-                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv>;
-    MIFGPU_REG_CASE(8, 8)
-    MIFGPU_REG_CASE(16, 8)
-    MIFGPU_REG_CASE(16, 16)
-    MIFGPU_REG_CASE(32, 16)
-    MIFGPU_REG_CASE(32, 32)
-#undef MIFGPU_REG_CASE
+  template <int A, int B>
+  static const void *pick(int mode, int kind) {
+    if (kind == 0)
+      return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 0>
+             : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 0>
+                                    : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 0>;
+    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 1>
+           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 1>
+                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 1>;
+  }
+  static const void *get(int n1, int n2, int mode, int kind) {
+    if (n1 == 8 && n2 == 8) return pick<8, 8>(mode, kind);
+    if (n1 == 16 && n2 == 8) return pick<16, 8>(mode, kind);
+    if (n1 == 16 && n2 == 16) return pick<16, 16>(mode, kind);
+    if (n1 == 32 && n2 == 16) return pick<32, 16>(mode, kind);
+    if (n1 == 32 && n2 == 32) return pick<32, 32>(mode, kind);
     return nullptr;
   }
 };
 
 template <typename T>
 static void launch_reg(int n1, int n2, int mode, unsigned grid, size_t smem, cudaStream_t stream, LineArgs<T> a) {
-  const void *fn = RegKernels<T>::get(n1, n2, mode);
+  const void *fn = RegKernels<T>::get(n1, n2, mode, a.kind);
   void *args[] = {&a};
   cudaLaunchKernel(fn, dim3(grid), dim3(kThreads), args, smem, stream);
 }
@@ -605,7 +642,7 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
   for (int d = 0; d < 3; ++d) {
     if (!axis[d].reg_n1) continue;
     for (int mode = 0; mode < 3; ++mode) {
-      const void *fn = RegKernels<T>::get(axis[d].reg_n1, axis[d].reg_n2, mode);
+      const void *fn = RegKernels<T>::get(axis[d].reg_n1, axis[d].reg_n2, mode, axis[d].kind);
       if (!fn || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis[d].reg_smem) !=
                      cudaSuccess) {
         err = "register-path kernel set-up failed";

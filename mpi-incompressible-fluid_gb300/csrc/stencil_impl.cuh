@@ -105,9 +105,17 @@ struct StageCoef {
 };
 
 // One RK stage for all three components; ST selects the update formula.
+// Stage update at one point (all three components).
+template <typename T, int ST>
+__device__ __forceinline__ void stage_point(const Geometry &g, const Coeffs<T> &co, const Fields<T> &F,
+                                            const StageCoef<T> &K, int forcing, const ForcingEval<T> &fe, int i, int j,
+                                            int k);
+
+// One RK stage; each thread updates the points (i, j, k) and (i, j, k + kh),
+// whose loads are independent, so twice as many are in flight per thread.
 template <typename T, int ST>
 __global__ void __launch_bounds__(128) stage_kernel(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
-                                                    int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot) {
+                                                    int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot, int kh) {
   if (forcing) {
     fe.st = T(tr.get(sin_slot));
     fe.ct = T(tr.get(sin_slot + 1));
@@ -115,6 +123,14 @@ __global__ void __launch_bounds__(128) stage_kernel(Geometry g, Coeffs<T> co, Fi
   const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
   const int k = 1 + blockIdx.z;
+  stage_point<T, ST>(g, co, F, K, forcing, fe, i, j, k);
+  if (k + kh < g.Es[2] - 1) stage_point<T, ST>(g, co, F, K, forcing, fe, i, j, k + kh);
+}
+
+template <typename T, int ST>
+__device__ __forceinline__ void stage_point(const Geometry &g, const Coeffs<T> &co, const Fields<T> &F,
+                                            const StageCoef<T> &K, int forcing, const ForcingEval<T> &fe, int i, int j,
+                                            int k) {
   const long sy = g.sy(), sz = g.sz();
   const long q = g.idx(i, j, k);
   // The velocity set the right-hand side is computed from.
@@ -503,7 +519,8 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches) {
   const dim3 blk(32, 4, 1);
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
-  const dim3 grid(cdiv(ni - 2, 32), cdiv(g.Es[1] - 2, 4), (unsigned)(g.Es[2] - 2));
+  const int nk = g.Es[2] - 2, kh = (nk + 1) / 2;  // two points per thread: k and k + kh
+  const dim3 grid(cdiv(ni - 2, 32), cdiv(g.Es[1] - 2, 4), (unsigned)kh);
   const double dt = sc.dt;
   StageCoef<T> K{};
   switch (st) {
@@ -546,12 +563,12 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   const int forcing = sc.forcing != 0 && field_kind == kFieldSincos && ft.tab != nullptr;
   const Coeffs<T> co = make_coeffs<T>(g);
   switch (st) {
-    case kStageY2: stage_kernel<T, kStageY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
-    case kStageY3: stage_kernel<T, kStageY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
-    case kStageUStar: stage_kernel<T, kStageUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
-    case kVelY2: stage_kernel<T, kVelY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
-    case kVelY3: stage_kernel<T, kVelY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
-    default: stage_kernel<T, kVelUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot); break;
+    case kStageY2: stage_kernel<T, kStageY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
+    case kStageY3: stage_kernel<T, kStageY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
+    case kStageUStar: stage_kernel<T, kStageUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
+    case kVelY2: stage_kernel<T, kVelY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
+    case kVelY3: stage_kernel<T, kVelY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
+    default: stage_kernel<T, kVelUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
   }
   if (launches) ++*launches;
 }
