@@ -157,6 +157,14 @@ def allreduce_max(x, world):
     return float(t.item())
 
 
+def replica_throughput(ms_local: float, world: int, cells: int, steps: int) -> tuple:
+    """Whole-job throughput of `world` independent replicas: every rank did
+    `cells * steps` cell-steps; the job took the slowest rank's time.
+    Returns (Gcell-steps/s, max ms)."""
+    ms = allreduce_max(ms_local, world)
+    return world * cells * steps / (ms / 1e3) / 1e9, ms
+
+
 # ---------------------------------------------------------------- CPU baseline
 
 def _cpu_worker(args):
@@ -245,10 +253,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
     barrier(world)
     t += args.steps * dt
-    ms = e0.elapsed_time(e1)
-    ms = allreduce_max(ms, world)
+    value, ms = replica_throughput(e0.elapsed_time(e1), world, cells, args.steps)
     launches = s.launch_count() - launches0
-    value = world * cells * args.steps / (ms / 1e3) / 1e9
 
     # error against the analytic solution after the run (matched-error report)
     linf = None

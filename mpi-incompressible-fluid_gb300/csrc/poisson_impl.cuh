@@ -280,22 +280,6 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
 
-// The pair (a[m], b[m]) of the CTA's line pair: from the shared-memory row
-// (strided axes) or straight from global memory (contiguous x lines).
-template <typename T>
-struct PairSource {
-  const typename Vec2<T>::type *row;  // strided axes: staged row
-  const LineArgs<T> *a;               // x lines: global rows
-  long off_a, off_b;
-  __device__ __forceinline__ typename Vec2<T>::type operator()(int m) const {
-    if (row) return row[m];
-    typename Vec2<T>::type v;
-    v.x = off_a >= 0 ? line_value(*a, off_a + m) : T(0);
-    v.y = off_b >= 0 ? line_value(*a, off_b + m) : T(0);
-    return v;
-  }
-};
-
 // Element m of the first FFT's input: the even extension (DCT-I), the plain
 // pair (R2HC), or Z_k = A_k + i B_k rebuilt from two half-complex lines (HC2R).
 template <typename T2, typename Src>
@@ -407,9 +391,29 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
   const int nl = 2 * a.P;
 
   fill_line_table(table, a, line0, total);
-  if (a.line_fast) {
-    // Strided lines: stage the 2P x n tile asynchronously, consecutive threads
-    // on consecutive lines (consecutive addresses).
+  if (a.du) {
+    // x-forward fused with the divergence: contiguous rows, four elements
+    // per thread per iteration so their 24 loads are in flight together.
+    for (int l = 0; l < nl; ++l) {
+      const long off = table.off[l];
+      T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
+      for (int m0 = threadIdx.x; m0 < n; m0 += 4 * blockDim.x) {
+        T v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int m = m0 + u * blockDim.x;
+          v[u] = (off >= 0 && m < n) ? line_value(a, off + m) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int m = m0 + u * blockDim.x;
+          if (m < n) dst[2 * m] = v[u];
+        }
+      }
+    }
+  } else if (a.line_fast) {
+    // Strided lines: consecutive threads on consecutive lines (consecutive
+    // addresses), copied asynchronously.
     const int cnt = nl * n;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int m = e >> a.lg_lines, l = e & (nl - 1);
@@ -420,10 +424,22 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
       else
         *dst = T(0);
     }
-    cp_async_wait_all();
-    __syncthreads();
+  } else {
+    // Contiguous x lines, copied asynchronously row by row.
+    for (int l = 0; l < nl; ++l) {
+      const long off = table.off[l];
+      T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
+      for (int m = threadIdx.x; m < n; m += blockDim.x) {
+        if (off >= 0)
+          cp_async4(dst + 2 * m, a.data + off + m);
+        else
+          dst[2 * m] = T(0);
+      }
+    }
   }
-  PairSource<T> src{a.line_fast ? row : nullptr, &a, table.off[2 * pp], table.off[2 * pp + 1]};
+  cp_async_wait_all();
+  __syncthreads();
+  const T2 *src = row;
   const T *ea = nullptr, *eb = nullptr;
   if (MODE == kModeFwdEigInv) ea = a.eig + table.eoff[2 * pp] * n, eb = a.eig + table.eoff[2 * pp + 1] * n;
   constexpr int npass = MODE == kModeFwdEigInv ? 2 : 1;
@@ -440,7 +456,7 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
 #pragma unroll
     for (int n1 = 0; n1 < N1; ++n1) {
       const int m = n1 * N2 + t;
-      T2 v = pass == 0 ? reg_input<T2>(src, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
+      T2 v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
                        : row[KIND == 0 ? (m < n ? m : L - m) : m];
       if (plus) v.y = -v.y;
       x[n1] = v;
