@@ -61,7 +61,10 @@ enum mifgpu_forcing {
   MIFGPU_FORCING_NONE = 0,
   MIFGPU_FORCING_VELOCITY = 1,     /* u_t + (u.grad)u - lap(u)/Re of the SINCOS velocity,
                                       include/MomentumEquationForcing.h:10-32 */
-  MIFGPU_FORCING_NAVIER_STOKES = 2 /* the same plus grad p of the SINCOS pressure */
+  MIFGPU_FORCING_NAVIER_STOKES = 2, /* the same plus grad p of the SINCOS pressure */
+  MIFGPU_FORCING_TAYLOR_GREEN = 3    /* alpha * (sin x cos y cos z, -cos x sin y cos z, 0),
+                                        alpha = forcing_amplitude (a body force for the
+                                        periodic-box gradient runs) */
 };
 
 typedef struct {
@@ -76,6 +79,7 @@ typedef struct {
   int precision;     /* enum mifgpu_precision */
   int boundary_kind; /* enum mifgpu_field_kind: exact velocity on Dirichlet faces */
   int forcing;       /* enum mifgpu_forcing */
+  double forcing_amplitude; /* alpha of MIFGPU_FORCING_TAYLOR_GREEN */
 } mifgpu_params;
 
 typedef struct mifgpu_ctx mifgpu_ctx;

@@ -39,6 +39,7 @@ struct Constants {
   int precision = MIFGPU_FP64;
   int boundary_kind = MIFGPU_FIELD_ZERO;
   int forcing = MIFGPU_FORCING_NONE;
+  double forcing_amplitude = 0.0;
 };
 
 // Owns the device state: what the reference holds in Constants,
@@ -58,6 +59,7 @@ class Solver {
     p.precision = c.precision;
     p.boundary_kind = c.boundary_kind;
     p.forcing = c.forcing;
+    p.forcing_amplitude = c.forcing_amplitude;
     const int rc = mifgpu_create(&p, &ctx_);
     if (rc != MIFGPU_OK) {
       const std::string msg = ctx_ ? mifgpu_last_error(ctx_) : "invalid parameters";

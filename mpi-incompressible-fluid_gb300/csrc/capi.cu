@@ -307,7 +307,7 @@ struct Impl final : ImplBase {
     ForcingTables<T> ft{ftab, ftab_maxE};
     const int kind = ctx->prm.boundary_kind;
     if (variant == kVariantVelocity) {
-      StageScalars<T> sc{dt, 4, 1};
+      StageScalars<T> sc{dt, 4, 1, 0.0};
       launch_stage<T>(g, F, kVelY2, sc, ft, kind, tref(), s, cnt);
       enqueue_bc(ctx, s, 1, 1, cnt);
       sc.sin_slot = 6;
@@ -324,7 +324,7 @@ struct Impl final : ImplBase {
     const int out_set[3] = {1, 2, 0};
     const int sin_slot[3] = {4, 6, 8};
     for (int st = 0; st < 3; ++st) {
-      StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing};
+      StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing, ctx->prm.forcing_amplitude};
       mark(MIFGPU_PROF_STAGE, s);
       launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt);
       enqueue_bc(ctx, s, out_set[st], 1 + st, cnt);
@@ -478,7 +478,7 @@ int mifgpu_create(const mifgpu_params *p, mifgpu_ctx **out) {
   ctx->prm = *p;
   if (p->precision != MIFGPU_FP64 && p->precision != MIFGPU_MIXED)
     return MIFGPU_EINVAL;
-  if (p->boundary_kind < 0 || p->boundary_kind > 2 || p->forcing < 0 || p->forcing > 2) return MIFGPU_EINVAL;
+  if (p->boundary_kind < 0 || p->boundary_kind > 2 || p->forcing < 0 || p->forcing > 3) return MIFGPU_EINVAL;
   if (!(p->Re > 0) || !(p->dt > 0)) return MIFGPU_EINVAL;
   Geometry &g = ctx->g;
   for (int d = 0; d < 3; ++d) {

@@ -392,22 +392,29 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
 
   fill_line_table(table, a, line0, total);
   if (a.du) {
-    // x-forward fused with the divergence: contiguous rows, four elements
-    // per thread per iteration so their 24 loads are in flight together.
-    for (int l = 0; l < nl; ++l) {
-      const long off = table.off[l];
-      T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
-      for (int m0 = threadIdx.x; m0 < n; m0 += 4 * blockDim.x) {
-        T v[4];
+    // x-forward fused with the divergence: the CTA's nl x n elements as one
+    // flat range, eight per thread per round so their 48 loads are in flight
+    // together (consecutive threads on consecutive x: coalesced).
+    const int cnt = nl * n;
+    constexpr int U = 8;
+    for (int e0 = threadIdx.x; e0 < cnt; e0 += U * blockDim.x) {
+      T v[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int m = m0 + u * blockDim.x;
-          v[u] = (off >= 0 && m < n) ? line_value(a, off + m) : T(0);
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * blockDim.x;
+        v[u] = T(0);
+        if (e < cnt) {
+          const int l = e / n, m = e - l * n;
+          const long off = table.off[l];
+          if (off >= 0) v[u] = line_value(a, off + m);
         }
+      }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int m = m0 + u * blockDim.x;
-          if (m < n) dst[2 * m] = v[u];
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * blockDim.x;
+        if (e < cnt) {
+          const int l = e / n, m = e - l * n;
+          reinterpret_cast<T *>(s + (l >> 1) * ROW + m)[l & 1] = v[u];
         }
       }
     }
@@ -502,25 +509,36 @@ int smallest_radix(int L) {
 
 // ---- host side ----
 
-// (N1, N2) x mode x kind instantiations of the register path.
+// Kernel pointer of the register path for FFT shape (A, B), mode and kind.
+// Instantiated explicitly for float, one shape per translation unit
+// (poisson_reg_*.cu), so the shapes compile in parallel.
+template <typename T, int A, int B>
+const void *reg_kernel_ptr(int mode, int kind) {
+  if (kind == 0)
+    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 0>
+           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 0>
+                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 0>;
+  return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 1>
+         : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 1>
+                                : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 1>;
+}
+
+#define MIFGPU_REG_SHAPES(X) X(8, 8) X(16, 8) X(16, 16) X(32, 16) X(32, 32)
+#ifndef MIFGPU_REG_TU
+#define MIFGPU_REG_EXTERN(A, B) extern template const void *reg_kernel_ptr<float, A, B>(int, int);
+MIFGPU_REG_SHAPES(MIFGPU_REG_EXTERN)
+#undef MIFGPU_REG_EXTERN
+#endif
+
 template <typename T>
 struct RegKernels {
-  template <int A, int B>
-  static const void *pick(int mode, int kind) {
-    if (kind == 0)
-      return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 0>
-             : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 0>
-                                    : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 0>;
-    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 1>
-           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 1>
-                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 1>;
-  }
   static const void *get(int n1, int n2, int mode, int kind) {
-    if (n1 == 8 && n2 == 8) return pick<8, 8>(mode, kind);
-    if (n1 == 16 && n2 == 8) return pick<16, 8>(mode, kind);
-    if (n1 == 16 && n2 == 16) return pick<16, 16>(mode, kind);
-    if (n1 == 32 && n2 == 16) return pick<32, 16>(mode, kind);
-    if (n1 == 32 && n2 == 32) return pick<32, 32>(mode, kind);
+    if constexpr (std::is_same<T, float>::value) {
+#define MIFGPU_REG_GET(A, B) \
+  if (n1 == A && n2 == B) return reg_kernel_ptr<T, A, B>(mode, kind);
+      MIFGPU_REG_SHAPES(MIFGPU_REG_GET)
+#undef MIFGPU_REG_GET
+    }
     return nullptr;
   }
 };

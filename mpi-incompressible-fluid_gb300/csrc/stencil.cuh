@@ -45,7 +45,8 @@ template <typename T>
 struct StageScalars {
   double dt;     // Constants::dt
   int sin_slot;  // slot of sin(stage time); cos follows it
-  int forcing;   // 0 none, 1 velocity forcing, 2 with grad p
+  int forcing;   // 0 none, 1 velocity forcing, 2 with grad p, 3 Taylor-Green body force
+  double alpha;  // amplitude of the Taylor-Green body force
 };
 
 template <typename T>

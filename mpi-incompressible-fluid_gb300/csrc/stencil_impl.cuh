@@ -74,6 +74,8 @@ struct ForcingEval {
   int maxE;
   T st, ct, invRe;
   int with_p;
+  int tg;   // Taylor-Green body force alpha (sin x cos y cos z, -cos x sin y cos z, 0) instead
+  T alpha;
   __device__ __forceinline__ T S(int ax, int face, int i) const { return tab[((ax * 2 + face) * 2 + 0) * maxE + i]; }
   __device__ __forceinline__ T C(int ax, int face, int i) const { return tab[((ax * 2 + face) * 2 + 1) * maxE + i]; }
   __device__ __forceinline__ T operator()(int c, int i, int j, int k) const {
@@ -81,6 +83,7 @@ struct ForcingEval {
     const T sy = S(1, c == 1, j), cy = C(1, c == 1, j);
     const T sz = S(2, c == 2, k), cz = C(2, c == 2, k);
     T f;
+    if (tg) return c == 0 ? alpha * (sx * cy * cz) : (c == 1 ? -alpha * (cx * sy * cz) : T(0));
     if (c == 0) {
       f = sx * cy * sz * ct + st * st * sx * cx * (cy * cy * sz * sz - sy * sy * sz * sz + T(2) * cy * cy * cz * cz) +
           T(3) * sx * cy * sz * st * invRe;
@@ -178,6 +181,170 @@ __device__ __forceinline__ void stage_point(const Geometry &g, const Coeffs<T> &
       F.vel(1, c)[q] = r1 + K.k1 * (K.k2 * r);
     }
   }
+}
+
+// ---- 2.5D-tiled stage kernel ----
+//
+// A CTA owns a TX x TY tile of (i, j) and marches through kc planes of k. The
+// input velocity set and p live in a ring of four shared-memory planes per
+// field (k-1, k, k+1 and the plane being prefetched), each with a one-point
+// halo in x and y; plane k+2 is copied with cp.async while plane k is
+// computed. Every stencil neighbour of include/MomentumEquation.h then comes
+// from shared memory and each point costs about five global loads.
+constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kPL = kHX * kHY;
+
+__device__ __forceinline__ void cp_async4_st(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async8_st(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+template <typename T>
+struct Ring {
+  T f[4][4][kPL];  // field (u, v, w, p), slot (k & 3), tile
+};
+
+// Neighbour accessor on the ring: field f at (i + di, j + dj, k + dk).
+template <typename T>
+struct Tap {
+  const Ring<T> *r;
+  int k, base;  // base = (ty + 1) * kHX + tx + 1
+  __device__ __forceinline__ T operator()(int f, int di, int dj, int dk) const {
+    return r->f[f][(k + dk) & 3][base + dj * kHX + di];
+  }
+};
+
+// include/MomentumEquation.h:42-255 (OPT_CPU_CACHE branch) on the ring.
+template <typename T>
+__device__ __forceinline__ T rhs_tap(int c, const Tap<T> &A, const Coeffs<T> &co) {
+  if (c == 0) {
+    const T u13 = A(0, -1, 0, 0), u11 = A(0, 0, -1, 0), u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u23 = A(0, 0, 0, 1),
+            u17 = A(0, 0, 1, 0), u15 = A(0, 1, 0, 0);
+    const T v13 = A(1, -1, 0, 0), v16 = A(1, -1, 1, 0), v14 = A(1, 0, 0, 0), v17 = A(1, 0, 1, 0);
+    const T w13 = A(2, -1, 0, 0), w22 = A(2, -1, 0, 1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1);
+    const T conv = -u14 * (u15 - u13) * co.o2h[0] - (v17 + v14 + v16 + v13) * (u17 - u11) * co.o8h[1] -
+                   (w23 + w14 + w22 + w13) * (u23 - u5) * co.o8h[2];
+    const T diff = (u15 - T(2) * u14 + u13) * co.oh2Re[0] + (u17 - T(2) * u14 + u11) * co.oh2Re[1] +
+                   (u23 - T(2) * u14 + u5) * co.oh2Re[2];
+    return conv + diff;
+  }
+  if (c == 1) {
+    const T u11 = A(0, 0, -1, 0), u14 = A(0, 0, 0, 0), u12 = A(0, 1, -1, 0), u15 = A(0, 1, 0, 0);
+    const T v13 = A(1, -1, 0, 0), v11 = A(1, 0, -1, 0), v5 = A(1, 0, 0, -1), v14 = A(1, 0, 0, 0), v23 = A(1, 0, 0, 1),
+            v17 = A(1, 0, 1, 0), v15 = A(1, 1, 0, 0);
+    const T w11 = A(2, 0, -1, 0), w20 = A(2, 0, -1, 1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1);
+    const T conv = -(u15 + u14 + u12 + u11) * (v15 - v13) * co.o8h[0] - v14 * (v17 - v11) * co.o2h[1] -
+                   (w23 + w14 + w20 + w11) * (v23 - v5) * co.o8h[2];
+    const T diff = (v15 - T(2) * v14 + v13) * co.oh2Re[0] + (v17 - T(2) * v14 + v11) * co.oh2Re[1] +
+                   (v23 - T(2) * v14 + v5) * co.oh2Re[2];
+    return conv + diff;
+  }
+  const T u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u6 = A(0, 1, 0, -1), u15 = A(0, 1, 0, 0);
+  const T v5 = A(1, 0, 0, -1), v14 = A(1, 0, 0, 0), v8 = A(1, 0, 1, -1), v17 = A(1, 0, 1, 0);
+  const T w13 = A(2, -1, 0, 0), w11 = A(2, 0, -1, 0), w5 = A(2, 0, 0, -1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1),
+          w17 = A(2, 0, 1, 0), w15 = A(2, 1, 0, 0);
+  const T conv = -(u15 + u14 + u6 + u5) * (w15 - w13) * co.o8h[0] - (v17 + v14 + v8 + v5) * (w17 - w11) * co.o8h[1] -
+                 w14 * (w23 - w5) * co.o2h[2];
+  const T diff = (w15 - T(2) * w14 + w13) * co.oh2Re[0] + (w17 - T(2) * w14 + w11) * co.oh2Re[1] +
+                 (w23 - T(2) * w14 + w5) * co.oh2Re[2];
+  return conv + diff;
+}
+
+template <typename T, int ST>
+__global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
+                                                              int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot,
+                                                              int kc) {
+  constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
+  constexpr int in_set = (ST == kStageY2 || ST == kVelY2 || ST == kVelUStar) ? 0
+                         : (ST == kStageY3 || ST == kVelY3)                  ? 1
+                                                                             : 2;
+  __shared__ __align__(16) Ring<T> ring;
+  if (forcing) {
+    fe.st = T(tr.get(sin_slot));
+    fe.ct = T(tr.get(sin_slot + 1));
+  }
+  const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+  const int i0 = 1 + blockIdx.x * kTX, j0 = 1 + blockIdx.y * kTY;
+  const int zmax = g.Es[2] - 1;  // interior k < zmax
+  const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
+  const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
+  constexpr int nf = kUseP ? 4 : 3;
+  auto load_plane = [&](int kk) {
+    if (kk >= 0 && kk < g.PZ) {
+      for (int e = threadIdx.x; e < kPL; e += kTX * kTY) {
+        const int hx = e % kHX, hy = e / kHX;
+        const int i = i0 - 1 + hx, j = j0 - 1 + hy;
+        const bool ok = i < g.PX && j < g.PY;
+        const long q = g.idx(i, j, kk);
+#pragma unroll
+        for (int f = 0; f < nf; ++f) {
+          T *d = &ring.f[f][kk & 3][e];
+          if (ok)
+            cp_async4_st(d, src[f] + q);
+          else
+            *d = T(0);
+        }
+      }
+    }
+    cp_commit();
+  };
+  load_plane(kbeg - 1);
+  load_plane(kbeg);
+  load_plane(kbeg + 1);
+  const int i = i0 + tx, j = j0 + ty;
+  const long sy = g.sy(), sz = g.sz();
+  const Tap<T> base_tap{&ring, 0, (ty + 1) * kHX + tx + 1};
+  for (int k = kbeg; k < kend; ++k) {
+    load_plane(k + 2);
+    cp_wait1();
+    __syncthreads();
+    Tap<T> A = base_tap;
+    A.k = k;
+    const long q = g.idx(i, j, k);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
+      T r = rhs_tap(c, A, co);
+      if (forcing) r = r + fe(c, i, j, k);
+      T gp = T(0);
+      if (kUseP) {
+        const T pm = c == 0 ? A(3, -1, 0, 0) : (c == 1 ? A(3, 0, -1, 0) : A(3, 0, 0, -1));
+        gp = (A(3, 0, 0, 0) - pm) * co.oh[c];
+      }
+      const T self = A(c, 0, 0, 0);  // the input set's own value at the point
+      if (ST == kStageY2) {
+        F.vel(1, c)[q] = self + K.k1 * r - K.k3 * gp;
+        F.vel(2, c)[q] = r;
+      } else if (ST == kStageY3) {
+        const T r1 = F.vel(2, c)[q];
+        const T r2s = K.k2 * r;
+        F.vel(2, c)[q] = self + K.k1 * r1 + r2s - K.k3 * gp;
+        F.vel(0, c)[q] = r2s;
+      } else if (ST == kStageUStar) {
+        const T r2s = -F.vel(0, c)[q];
+        F.vel(0, c)[q] = self + r2s + K.k2 * r - K.k3 * gp;
+      } else if (ST == kVelY2) {
+        F.vel(2, c)[q] = r;
+        F.vel(1, c)[q] = self + K.k1 * r;
+      } else if (ST == kVelY3) {
+        const T r1 = F.vel(2, c)[q];
+        const T uu = F.vel(0, c)[q];
+        F.vel(2, c)[q] = uu + K.k1 * (K.k2 * r1);
+        F.vel(0, c)[q] = uu + K.k1 * (K.k3 * r1 + K.k4 * r);
+      } else {
+        const T r1 = F.vel(2, c)[q];
+        F.vel(1, c)[q] = r1 + K.k1 * (K.k2 * r);
+      }
+    }
+    __syncthreads();  // the next iteration refills the slot of plane k - 1
+  }
+  (void)sy;
+  (void)sz;
 }
 
 // ---- boundary fill, src/VelocityTensor.cpp:36-233 ----
@@ -517,10 +684,10 @@ Coeffs<T> make_coeffs(const Geometry &g) {
 template <typename T>
 void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches) {
-  const dim3 blk(32, 4, 1);
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
-  const int nk = g.Es[2] - 2, kh = (nk + 1) / 2;  // two points per thread: k and k + kh
-  const dim3 grid(cdiv(ni - 2, 32), cdiv(g.Es[1] - 2, 4), (unsigned)kh);
+  const int nk = g.Es[2] - 2;
+  const int kc = 32;  // planes per CTA
+  const dim3 tgrid(cdiv(ni - 2, kTX), cdiv(g.Es[1] - 2, kTY), cdiv(nk, kc));
   const double dt = sc.dt;
   StageCoef<T> K{};
   switch (st) {
@@ -560,15 +727,18 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   fe.ct = T(0);
   fe.invRe = T(1.0 / g.Re);
   fe.with_p = sc.forcing == 2;
-  const int forcing = sc.forcing != 0 && field_kind == kFieldSincos && ft.tab != nullptr;
+  fe.tg = sc.forcing == 3;
+  fe.alpha = T(sc.alpha);
+  const int forcing = ft.tab != nullptr && ((sc.forcing == 1 || sc.forcing == 2) ? field_kind == kFieldSincos
+                                                                                  : sc.forcing == 3);
   const Coeffs<T> co = make_coeffs<T>(g);
   switch (st) {
-    case kStageY2: stage_kernel<T, kStageY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
-    case kStageY3: stage_kernel<T, kStageY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
-    case kStageUStar: stage_kernel<T, kStageUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
-    case kVelY2: stage_kernel<T, kVelY2><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
-    case kVelY3: stage_kernel<T, kVelY3><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
-    default: stage_kernel<T, kVelUStar><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kh); break;
+    case kStageY2: stage_kernel_tiled<T, kStageY2><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
+    case kStageY3: stage_kernel_tiled<T, kStageY3><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
+    case kStageUStar: stage_kernel_tiled<T, kStageUStar><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
+    case kVelY2: stage_kernel_tiled<T, kVelY2><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
+    case kVelY3: stage_kernel_tiled<T, kVelY3><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
+    default: stage_kernel_tiled<T, kVelUStar><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
   }
   if (launches) ++*launches;
 }

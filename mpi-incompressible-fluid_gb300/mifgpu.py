@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "libmifgpu.so")
 FIELDS = {"u": 0, "v": 1, "w": 2, "u1": 3, "v1": 4, "w1": 5, "u2": 6, "v2": 7, "w2": 8, "p": 9, "phi": 10}
 FP64, MIXED = 0, 1
 FIELD_ZERO, FIELD_SINCOS, FIELD_ETHIER = 0, 1, 2
-FORCING_NONE, FORCING_VELOCITY, FORCING_NAVIER_STOKES = 0, 1, 2
+FORCING_NONE, FORCING_VELOCITY, FORCING_NAVIER_STOKES, FORCING_TAYLOR_GREEN = 0, 1, 2, 3
 
 EXPORTED = [
     "mifgpu_create", "mifgpu_destroy", "mifgpu_set_stream", "mifgpu_synchronize", "mifgpu_last_error",
@@ -54,6 +54,7 @@ class Params(C.Structure):
         ("precision", C.c_int),
         ("boundary_kind", C.c_int),
         ("forcing", C.c_int),
+        ("forcing_amplitude", C.c_double),
     ]
 
 
@@ -108,7 +109,8 @@ class Solver:
     """One device-resident solver state (the reference's Constants + tensors)."""
 
     def __init__(self, n_global, size=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), Re=1000.0, dt=1e-4,
-                 periodic=(False, False, False), precision=FP64, boundary_kind=FIELD_ZERO, forcing=FORCING_NONE):
+                 periodic=(False, False, False), precision=FP64, boundary_kind=FIELD_ZERO, forcing=FORCING_NONE,
+                 forcing_amplitude=0.0):
         self.lib = load_library()
         p = Params()
         for k in range(3):
@@ -118,6 +120,7 @@ class Solver:
             p.periodic[k] = 1 if periodic[k] else 0
         p.Re, p.dt = float(Re), float(dt)
         p.precision, p.boundary_kind, p.forcing = int(precision), int(boundary_kind), int(forcing)
+        p.forcing_amplitude = float(forcing_amplitude)
         self.params = p
         self.dt = float(dt)
         h = C.c_void_p()
