@@ -212,6 +212,118 @@ def cpu_baseline(workers: int, n: int = 97, steps: int = 3):
                       f"(wall {wall:.1f}s)"}
 
 
+# ------------------------------------------------------------------ adjoint workload
+
+ADJOINT = dict(n=128, L=2 * 3.141592653589793, Re=500.0, dt=2e-3, nsteps=200, every=20, kmax=8, amp=1.0,
+               alpha=0.5, seed=1234)
+
+
+def random_solenoidal(shape_of, n, L, kmax, amp, seed):
+    """Seeded divergence-free velocity on the periodic staggered grid: the curl of
+    a Gaussian vector potential with |A_k| ~ |k|^-2 (|k| <= kmax), scaled to max |u| = amp.
+
+    Each component is sampled at its own staggered points (offset -h/2 along
+    its axis) by a spectral phase shift; ghost points are periodic copies."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    k1 = np.fft.fftfreq(n, d=1.0 / n)
+    kx, ky, kz = np.meshgrid(k1, k1, k1, indexing="ij")
+    kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    mask = (kk > 0) & (kk <= kmax)
+    spec = np.where(mask, 1.0 / np.maximum(kk, 1.0) ** 2, 0.0)
+    A = [np.fft.fftn(rng.standard_normal((n, n, n))) * spec for _ in range(3)]
+    w = 2 * np.pi / L
+    K = (kx * w, ky * w, kz * w)
+    uh = (1j * (K[1] * A[2] - K[2] * A[1]), 1j * (K[2] * A[0] - K[0] * A[2]), 1j * (K[0] * A[1] - K[1] * A[0]))
+    h = L / n
+    out = {}
+    vals = []
+    for c, name in enumerate("uvw"):
+        shifted = uh[c] * np.exp(-1j * K[c] * h / 2)
+        f = np.real(np.fft.ifftn(shifted))  # f[ix, iy, iz] at x = ix h (- h/2 along c)
+        vals.append(f)
+    scale = amp / max(np.abs(f).max() for f in vals)
+    for c, name in enumerate("uvw"):
+        ez, ey, ex = shape_of(name)
+        ii = (np.arange(ex) - 1) % n
+        jj = (np.arange(ey) - 1) % n
+        kq = (np.arange(ez) - 1) % n
+        f = vals[c] * scale
+        out[name] = np.ascontiguousarray(f[np.ix_(ii, jj, kq)].transpose(2, 1, 0))
+    return out
+
+
+def adjoint_bench(stream):
+    """Checkpointed gradient of the kinetic energy in [pi/2, 3pi/2]^3 after 200
+    steps of a periodic 128^3 box, in FP32 and FP64: cost against the forward
+    steps, FP32 gradient error against FP64, and an FP64 dot-product test."""
+    import numpy as np
+    import torch
+
+    import mifgpu
+
+    a = ADJOINT
+    n = a["n"]
+    pi = 3.141592653589793
+    box = (pi / 2, 3 * pi / 2) * 3
+    res = {"workload": f"periodic {n}^3 box [0,2pi]^3, Re={a['Re']}, dt={a['dt']}, {a['nsteps']} steps, "
+                       f"checkpoint every {a['every']}, Taylor-Green forcing alpha={a['alpha']}, "
+                       f"k^-2 solenoidal initial velocity |k|<={a['kmax']} max|u|={a['amp']}",
+           "loss": "kinetic energy in [pi/2,3pi/2]^3 at the final time"}
+    grads = {}
+    for prec_name, prec in (("fp32", mifgpu.MIXED), ("fp64", mifgpu.FP64)):
+        s = mifgpu.Solver(n_global=(n + 1,) * 3, size=(a["L"],) * 3, Re=a["Re"], dt=a["dt"],
+                          periodic=(True, True, True), precision=prec, forcing=mifgpu.FORCING_TAYLOR_GREEN,
+                          forcing_amplitude=a["alpha"])
+        s.set_stream(stream.cuda_stream)
+        st = random_solenoidal(s.shape, n, a["L"], a["kmax"], a["amp"], a["seed"])
+        st["p"] = np.zeros(s.shape("p"))
+        s.load_state(st)
+        s.run(0.0, 3)  # warm-up, graph capture
+        s.load_state(st)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.run(0.0, a["nsteps"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fwd_ms = e0.elapsed_time(e1) / a["nsteps"]
+        s.load_state(st)
+        r = s.gradient_ke(0.0, a["nsteps"], a["every"], box)
+        g = {nm: s.adjoint(nm) for nm in "uvwp"}
+        grads[prec_name] = (r, g)
+        rev = r["reverse_ms"] / a["nsteps"]
+        rec = r["recompute_ms"] / a["nsteps"]
+        out = {"forward_ms_per_step": round(fwd_ms, 4), "reverse_ms_per_step": round(rev, 4),
+               "recompute_ms_per_step": round(rec, 4),
+               "adjoint_step_ratio": round(rev / fwd_ms, 3),
+               "backward_ratio": round((rev + rec) / fwd_ms, 3),
+               "gradient_pass_ratio": round((r["forward_ms"] + r["recompute_ms"] + r["reverse_ms"]) /
+                                            (fwd_ms * a["nsteps"]), 3),
+               "loss": r["loss"], "dloss_dalpha": r["dloss_dalpha"], "device_gb": round(s.device_bytes() / 1e9, 2)}
+        if prec == mifgpu.FP64:
+            # dot-product test against the tangent-linear derivative (central difference)
+            rng = np.random.default_rng(5)
+            delta = {nm: rng.standard_normal(st[nm].shape) for nm in "uvw"}
+            adj = sum(float(np.sum(g[nm] * delta[nm])) for nm in "uvw")
+            eps = 1e-6
+            ls = []
+            for sign in (1, -1):
+                s.load_state({nm: st[nm] + sign * eps * delta[nm] for nm in "uvw"} | {"p": st["p"]})
+                ls.append(s.gradient_ke(0.0, a["nsteps"], a["every"], box)["loss"])
+            tl = (ls[0] - ls[1]) / (2 * eps)
+            out["dot_product_rel_err"] = abs(tl - adj) / abs(tl)
+        res[prec_name] = out
+        s.close()
+        torch.cuda.empty_cache()
+    (r32, g32), (r64, g64) = grads["fp32"], grads["fp64"]
+    res["fp32_vs_fp64_gradient_max_rel_err"] = max(
+        float(np.abs(g32[nm] - g64[nm]).max() / np.abs(g64[nm]).max()) for nm in "uvw")
+    res["fp32_vs_fp64_dalpha_rel_err"] = abs(r32["dloss_dalpha"] - r64["dloss_dalpha"]) / abs(r64["dloss_dalpha"])
+    return res
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def run_gpu(args):
@@ -338,6 +450,12 @@ def run_gpu(args):
             fp64["t"] = t64
         s64.close()
 
+    adjoint = None
+    if not args.no_adjoint:
+        s.close()
+        torch.cuda.empty_cache()
+        adjoint = adjoint_bench(stream)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(workers=1)
@@ -355,7 +473,7 @@ def run_gpu(args):
             "step_roofline": {"bytes_per_cell_step": STEP_SWEEPS * elem, "achieved_gbs": round(step_roofline, 1),
                               "frac": round(step_roofline / peak, 4)},
             "kernel_ms_per_step": {k: round(v, 4) for k, v in prof.items()},
-            "error": linf, "fp64": fp64, "cpu_baseline": cpu,
+            "error": linf, "fp64": fp64, "adjoint": adjoint, "cpu_baseline": cpu,
         }
         print(json.dumps(line))
 
@@ -396,6 +514,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -180,6 +180,43 @@ enum mifgpu_prof_class {
  * fields advance. No counterpart in the reference (instrumentation). */
 int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIFGPU_PROF_CLASSES]);
 
+/* ---- Reverse mode (no counterpart in the reference) ----
+ *
+ * Discrete adjoint of `nsteps` projection steps of mifgpu_run from the
+ * context's current state at t0 (velocity set 0 and the pressure are the
+ * inputs; sets 1, 2 and phi are scratch, as in the reference). The forward
+ * pass stores (u, v, w, p) every `checkpoint_every` steps (1..1024); the
+ * backward pass recomputes one segment at a time, keeping the three sets each
+ * stage's right-hand side was evaluated at, and runs the transposed step
+ * kernels in reverse. Device memory: 11 adjoint fields + 4 per checkpoint
+ * (nsteps / checkpoint_every + 2 of them) + 9 per step of a segment.
+ *
+ * On return the context holds the final state, and mifgpu_download_adjoint
+ * gives d loss / d (initial field) for field ids 0, 1, 2 (u, v, w of set 0,
+ * every point of their extents, ghosts included) and 9 (pressure).
+ * `dloss_dalpha` (may be null) receives the derivative with respect to
+ * forcing_amplitude when the forcing is MIFGPU_FORCING_TAYLOR_GREEN, else 0.
+ * `ms_out` (may be null) receives milliseconds of the forward pass, the
+ * segment recomputes and the reverse sweeps, timed with CUDA events. */
+
+/* Loss = 1/2 hx hy hz * sum of u_c^2 over the interior staggered points of
+ * each component whose position lies in box = {x0, x1, y0, y1, z0, z1}
+ * (the kinetic energy in a sub-box at the final time). */
+int mifgpu_gradient_ke(mifgpu_ctx *ctx, double t0, int nsteps, int checkpoint_every, const double box[6],
+                       double *loss, double *dloss_dalpha, double ms_out[3]);
+
+/* The same for a caller-defined loss: seed_{u,v,w,p} are d loss / d (final
+ * field) in the reference layout (null = zero). */
+int mifgpu_backward(mifgpu_ctx *ctx, double t0, int nsteps, int checkpoint_every, const double *seed_u,
+                    const double *seed_v, const double *seed_w, const double *seed_p, double *dloss_dalpha,
+                    double ms_out[3]);
+
+/* d loss / d (initial field) of the last mifgpu_gradient_ke / mifgpu_backward. */
+int mifgpu_download_adjoint(mifgpu_ctx *ctx, int field, double *host);
+
+/* Changes alpha of the Taylor-Green forcing (re-captures the step graphs). */
+int mifgpu_set_forcing_amplitude(mifgpu_ctx *ctx, double alpha);
+
 /* Number of kernels this context has launched so far (for launch accounting). */
 int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out);
 

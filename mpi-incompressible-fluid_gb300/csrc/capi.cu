@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/mifgpu.h"
+#include "adjoint_impl.cuh"
 #include "common.cuh"
 #include "poisson.cuh"
 #include "stencil.cuh"
@@ -22,6 +23,17 @@
 using namespace mifgpu;
 
 namespace {
+
+// One reverse-mode request: nsteps projection steps from the context's
+// state at t0, a loss on the final state, and its back-propagation.
+struct GradRequest {
+  double t0 = 0;
+  int nsteps = 0;
+  int every = 1;                                        // checkpoint interval (steps)
+  const double *box = nullptr;                          // kinetic-energy loss box, or null
+  const double *seed[4] = {nullptr, nullptr, nullptr, nullptr};  // host d loss / d (u, v, w, p) otherwise
+  double *loss = nullptr, *dalpha = nullptr, *ms = nullptr;
+};
 
 struct ImplBase {
   virtual ~ImplBase() = default;
@@ -39,6 +51,9 @@ struct ImplBase {
   virtual int profile_step(mifgpu_ctx *ctx, double t_n, int reps, double *ms) = 0;
   virtual void swap_sets() = 0;
   virtual size_t bytes() const = 0;
+  virtual int gradient(mifgpu_ctx *ctx, const GradRequest &req) = 0;
+  virtual int download_adjoint(mifgpu_ctx *ctx, int id, double *host) = 0;
+  virtual void drop_graphs() = 0;
 };
 
 }  // namespace
@@ -147,6 +162,15 @@ struct Impl final : ImplBase {
   size_t total_bytes = 0;
   // Per-kernel-class event marks of a profiled (non-graph) step.
   std::vector<std::pair<int, cudaEvent_t>> *prof = nullptr;
+  // Reverse mode: the adjoint fields (lx 3, mu 3, pend 3, rho, lp), the
+  // checkpoints (u, v, w, p per segment start and the final state) and the
+  // per-step snapshots of one segment (the three sets each stage's
+  // right-hand side was evaluated at).
+  T *adj_block = nullptr;
+  T *ckpt_block = nullptr;
+  size_t ckpt_fields = 0;
+  T *snap_block = nullptr;
+  size_t snap_fields = 0;
 
   void mark(int cls, cudaStream_t s) {
     if (!prof) return;
@@ -168,6 +192,9 @@ struct Impl final : ImplBase {
     cudaFree(acc);
     cudaFree(staging);
     cudaFree(grad_block);
+    cudaFree(adj_block);
+    cudaFree(ckpt_block);
+    cudaFree(snap_block);
     if (cap_stream) cudaStreamDestroy(cap_stream);
   }
 
@@ -462,6 +489,200 @@ struct Impl final : ImplBase {
     return MIFGPU_OK;
   }
 
+  // ---- reverse mode ----
+
+  T *adj_field(int q) const { return adj_block + (size_t)q * field_elems; }
+  enum { kLX = 0, kMU = 3, kPEND = 6, kRHO = 9, kLP = 10, kAdjFields = 11 };
+
+  int ensure_fields(mifgpu_ctx *ctx, T *&buf, size_t &have, size_t need, const char *what) {
+    if (have >= need) return MIFGPU_OK;
+    cudaFree(buf);
+    buf = nullptr;
+    total_bytes -= sizeof(T) * field_elems * have;
+    have = 0;
+    if (cudaMalloc(&buf, sizeof(T) * field_elems * need) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, MIFGPU_ENOMEM, std::string("cudaMalloc of the ") + what + " failed");
+    }
+    have = need;
+    total_bytes += sizeof(T) * field_elems * need;
+    return MIFGPU_OK;
+  }
+
+  cudaError_t copy_fields(T *dst, const T *src, int n, cudaStream_t s) {
+    return cudaMemcpyAsync(dst, src, sizeof(T) * field_elems * n, cudaMemcpyDeviceToDevice, s);
+  }
+
+  // Adjoint of one projection step (src/Timestep.cpp:97-141) given the
+  // adjoint of its output in lx (velocity set 0) and lp (pressure), and the
+  // sets the three stage right-hand sides were evaluated at: V[0] = u_n,
+  // V[1] = set 1 and V[2] = set 2 after the step. Leaves the adjoint of the
+  // step's input in lx and lp and adds d loss / d alpha into *dalpha.
+  void reverse_step(mifgpu_ctx *ctx, cudaStream_t s, const T *const V[3][3], double *dalpha, long long *cnt) {
+    using Ops = AdjointOps<T>;
+    const double dt = g.dt;
+    T *lx[3] = {adj_field(kLX), adj_field(kLX + 1), adj_field(kLX + 2)};
+    T *mu[3] = {adj_field(kMU), adj_field(kMU + 1), adj_field(kMU + 2)};
+    T *pend[3] = {adj_field(kPEND), adj_field(kPEND + 1), adj_field(kPEND + 2)};
+    T *rho = adj_field(kRHO), *lp = adj_field(kLP);
+    // Stage k: projection step dt_k, weight of its own R, weight of grad p,
+    // and the weight of the previous stage's R that its update carries.
+    const double dts[3] = {64.0 / 120.0 * dt, 16.0 / 120.0 * dt, 40.0 / 120.0 * dt};
+    const double a_own[3] = {64.0 / 120.0 * dt, 50.0 / 120.0 * dt, 90.0 / 120.0 * dt};
+    const double b_p[3] = {64.0 / 120.0 * dt, 16.0 / 120.0 * dt, 40.0 / 120.0 * dt};
+    const double a_prev[3] = {0.0, -34.0 / 120.0 * dt, -50.0 / 120.0 * dt};
+    const bool tg = ctx->prm.forcing == MIFGPU_FORCING_TAYLOR_GREEN;
+    for (int st = 2; st >= 0; --st) {
+      // phi = P M D X / dt_k, p += phi, X -= dt_k G phi on the interior
+      Ops::grad_adjoint(g, rho, lp, lx, -dts[st], true, s, cnt);
+      Ops::periodic_scalar_adjoint(g, rho, s, cnt);
+      ps.solve(rho, s, cnt);
+      Ops::div_adjoint(g, lx, lx, rho, 1.0 / dts[st], s, cnt);
+      // boundary fill of the stage's output set
+      Ops::bc_adjoint(g, lx, s, cnt);
+      // X = prev + a_own R(prev) + a_prev R_prev - b_p G p on the interior
+      Ops::grad_adjoint(g, lp, lp, lx, -b_p[st], false, s, cnt);
+      Ops::split(g, mu, pend, lx, a_own[st], st < 2 ? 1.0 : 0.0, a_prev[st], st > 0, tg ? ftab : nullptr, ftab_maxE,
+                 dalpha, s, cnt);
+      Ops::rhs_adjoint(g, lx, mu, V[st], s, cnt);
+    }
+  }
+
+  int gradient(mifgpu_ctx *ctx, const GradRequest &req) override {
+    const int N = req.nsteps;
+    const int C = std::max(1, std::min(req.every, N));
+    if (C > slots_cap) return fail(ctx, MIFGPU_EINVAL, "checkpoint interval above 1024 steps");
+    const int nseg = (N + C - 1) / C;
+    size_t have_adj = adj_block ? (size_t)kAdjFields : 0;
+    if (int rc = ensure_fields(ctx, adj_block, have_adj, kAdjFields, "adjoint fields")) return rc;
+    if (int rc = ensure_fields(ctx, ckpt_block, ckpt_fields, (size_t)4 * (nseg + 1), "checkpoints")) return rc;
+    if (int rc = ensure_fields(ctx, snap_block, snap_fields, (size_t)9 * C, "segment snapshots")) return rc;
+    if (int rc = ensure_graph(ctx, kVariantProjection)) return rc;
+    cudaStream_t s = ctx->stream;
+    long long *cnt = &ctx->launches;
+    std::vector<double> sl((size_t)kSlotSize * N);
+    for (int n = 0; n < N; ++n) projection_slot(req.t0 + n * g.dt, g.dt, sl.data() + (size_t)kSlotSize * n);
+    T *set0 = F.vel(0, 0), *set1 = F.vel(1, 0), *set2 = F.vel(2, 0), *p = F.f[kP];
+    auto ck = [&](int seg) { return ckpt_block + (size_t)4 * seg * field_elems; };
+    auto sn = [&](int m) { return snap_block + (size_t)9 * m * field_elems; };
+    std::vector<std::pair<int, cudaEvent_t>> marks;
+    auto phase = [&](int ph) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      cudaEventRecord(e, s);
+      marks.push_back({ph, e});
+    };
+    auto cleanup = [&]() {
+      for (auto &m : marks) cudaEventDestroy(m.second);
+    };
+    auto run_seg = [&](int seg, bool snap) -> cudaError_t {
+      const int n0 = seg * C, len = std::min(C, N - n0);
+      cudaError_t e = cudaMemcpyAsync(slots, sl.data() + (size_t)kSlotSize * n0, sizeof(double) * kSlotSize * len,
+                                      cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(step_ctr, 0, sizeof(int), s);
+      for (int m = 0; m < len && e == cudaSuccess; ++m) {
+        if (snap) e = copy_fields(sn(m), set0, 3, s);
+        if (e == cudaSuccess) e = cudaGraphLaunch(graph[kVariantProjection][parity], s);
+        *cnt += graph_launches[kVariantProjection][parity];
+        if (snap && e == cudaSuccess) e = copy_fields(sn(m) + 3 * field_elems, set1, 3, s);
+        if (snap && e == cudaSuccess) e = copy_fields(sn(m) + 6 * field_elems, set2, 3, s);
+      }
+      return e;
+    };
+    // forward pass, one checkpoint per segment start and one of the final state
+    phase(0);
+    for (int seg = 0; seg < nseg; ++seg) {
+      cudaError_t e = copy_fields(ck(seg), set0, 3, s);
+      if (e == cudaSuccess) e = copy_fields(ck(seg) + 3 * field_elems, p, 1, s);
+      if (e == cudaSuccess) e = run_seg(seg, false);
+      if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "forward pass");
+    }
+    CK(copy_fields(ck(nseg), set0, 3, s));
+    CK(copy_fields(ck(nseg) + 3 * field_elems, p, 1, s));
+    phase(2);
+    // seed the adjoint of the final state
+    T *lx[3] = {adj_field(kLX), adj_field(kLX + 1), adj_field(kLX + 2)};
+    CK(cudaMemsetAsync(acc, 0, sizeof(double) * 2, s));
+    if (req.box) {
+      const T *u[3] = {set0, set0 + field_elems, set0 + 2 * field_elems};
+      AdjointOps<T>::ke_seed(g, u, lx, req.box, acc, s, cnt);
+      CK(cudaMemsetAsync(adj_field(kLP), 0, sizeof(T) * field_elems, s));
+    } else {
+      CK(cudaMemsetAsync(adj_block, 0, sizeof(T) * field_elems * kAdjFields, s));
+      if (int rc = ensure_staging(ctx)) return cleanup(), rc;
+      const int ids[4] = {0, 1, 2, kP};
+      T *dst[4] = {lx[0], lx[1], lx[2], adj_field(kLP)};
+      for (int q = 0; q < 4; ++q) {
+        if (!req.seed[q]) continue;
+        int e3[3];
+        field_extent(g, ids[q], e3);
+        const size_t n = (size_t)e3[0] * e3[1] * e3[2];
+        CK(cudaMemcpyAsync(staging, req.seed[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        launch_scatter<T>(g, dst[q], staging, e3[0], e3[1], e3[2], s, cnt);
+      }
+    }
+    // backward: per segment, recompute it with snapshots, then reverse its steps
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+      phase(1);
+      const int len = std::min(C, N - seg * C);
+      cudaError_t e = copy_fields(set0, ck(seg), 3, s);
+      if (e == cudaSuccess) e = copy_fields(p, ck(seg) + 3 * field_elems, 1, s);
+      if (e == cudaSuccess) e = run_seg(seg, true);
+      if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "segment recompute");
+      phase(2);
+      for (int m = len - 1; m >= 0; --m) {
+        const T *V[3][3];
+        for (int st = 0; st < 3; ++st)
+          for (int c = 0; c < 3; ++c) V[st][c] = sn(m) + (size_t)(3 * st + c) * field_elems;
+        reverse_step(ctx, s, V, acc + 1, cnt);
+      }
+    }
+    phase(3);
+    // leave the context at the final state
+    CK(copy_fields(set0, ck(nseg), 3, s));
+    CK(copy_fields(p, ck(nseg) + 3 * field_elems, 1, s));
+    double h[2];
+    CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s));
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "gradient");
+    if (req.loss) *req.loss = h[0];
+    if (req.dalpha) *req.dalpha = h[1];
+    if (req.ms) {
+      for (int q = 0; q < 3; ++q) req.ms[q] = 0.0;
+      for (size_t q = 0; q + 1 < marks.size(); ++q) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, marks[q].second, marks[q + 1].second);
+        if (marks[q].first < 3) req.ms[marks[q].first] += t;
+      }
+    }
+    cleanup();
+    return MIFGPU_OK;
+  }
+
+  int download_adjoint(mifgpu_ctx *ctx, int id, double *host) override {
+    if (!adj_block) return fail(ctx, MIFGPU_EINVAL, "no adjoint has been computed on this context");
+    int e[3];
+    field_extent(g, id, e);
+    if (int rc = ensure_staging(ctx)) return rc;
+    const size_t n = (size_t)e[0] * e[1] * e[2];
+    const T *src = id == kP ? adj_field(kLP) : adj_field(kLX + id);
+    launch_gather<T>(g, staging, src, e[0], e[1], e[2], ctx->stream, &ctx->launches);
+    CK(cudaMemcpyAsync(host, staging, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MIFGPU_OK;
+  }
+
+  // Captured graphs hold the stage scalars: drop them when one changes.
+  void drop_graphs() override {
+    for (auto &gv : graph)
+      for (auto &gx : gv)
+        if (gx) {
+          cudaGraphExecDestroy(gx);
+          gx = nullptr;
+        }
+  }
+
   size_t bytes() const override { return total_bytes; }
 };
 
@@ -657,6 +878,50 @@ int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]) {
 int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIFGPU_PROF_CLASSES]) {
   if (!ctx || !ms_out || reps < 1) return MIFGPU_EINVAL;
   return ctx->impl->profile_step(ctx, t_n, reps, ms_out);
+}
+
+int mifgpu_gradient_ke(mifgpu_ctx *ctx, double t0, int nsteps, int checkpoint_every, const double box[6],
+                       double *loss, double *dloss_dalpha, double ms_out[3]) {
+  if (!ctx || !box || nsteps < 1 || checkpoint_every < 1) return MIFGPU_EINVAL;
+  GradRequest r;
+  r.t0 = t0;
+  r.nsteps = nsteps;
+  r.every = checkpoint_every;
+  r.box = box;
+  r.loss = loss;
+  r.dalpha = dloss_dalpha;
+  r.ms = ms_out;
+  return ctx->impl->gradient(ctx, r);
+}
+
+int mifgpu_backward(mifgpu_ctx *ctx, double t0, int nsteps, int checkpoint_every, const double *seed_u,
+                    const double *seed_v, const double *seed_w, const double *seed_p, double *dloss_dalpha,
+                    double ms_out[3]) {
+  if (!ctx || nsteps < 1 || checkpoint_every < 1) return MIFGPU_EINVAL;
+  GradRequest r;
+  r.t0 = t0;
+  r.nsteps = nsteps;
+  r.every = checkpoint_every;
+  r.seed[0] = seed_u;
+  r.seed[1] = seed_v;
+  r.seed[2] = seed_w;
+  r.seed[3] = seed_p;
+  r.dalpha = dloss_dalpha;
+  r.ms = ms_out;
+  return ctx->impl->gradient(ctx, r);
+}
+
+int mifgpu_download_adjoint(mifgpu_ctx *ctx, int field, double *host) {
+  if (!ctx || !host || !(field == 0 || field == 1 || field == 2 || field == kP)) return MIFGPU_EINVAL;
+  return ctx->impl->download_adjoint(ctx, field, host);
+}
+
+int mifgpu_set_forcing_amplitude(mifgpu_ctx *ctx, double alpha) {
+  if (!ctx || !std::isfinite(alpha)) return MIFGPU_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->prm.forcing_amplitude = alpha;
+  ctx->impl->drop_graphs();
+  return MIFGPU_OK;
 }
 
 int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out) {

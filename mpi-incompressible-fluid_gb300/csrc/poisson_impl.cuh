@@ -377,6 +377,7 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
 
 template <typename T, int N1, int N2, int MODE, int KIND>
 __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
+  static_assert(sizeof(T) == 4, "the register path stages 4-byte elements");
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
   constexpr int ROW = RegShape<N1, N2>::ROW;

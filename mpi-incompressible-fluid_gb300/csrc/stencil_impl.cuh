@@ -201,6 +201,14 @@ __device__ __forceinline__ void cp_async8_st(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
 }
+// One element of T (4 or 8 bytes) into shared memory.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem) {
+  if constexpr (sizeof(T) == 8)
+    cp_async8_st(smem, gmem);
+  else
+    cp_async4_st(smem, gmem);
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
 
@@ -285,7 +293,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
         for (int f = 0; f < nf; ++f) {
           T *d = &ring.f[f][kk & 3][e];
           if (ok)
-            cp_async4_st(d, src[f] + q);
+            cp_async_elem(d, src[f] + q);
           else
             *d = T(0);
         }

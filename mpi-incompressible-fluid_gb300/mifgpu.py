@@ -33,7 +33,8 @@ EXPORTED = [
     "mifgpu_set_exact_pressure", "mifgpu_timestep", "mifgpu_run", "mifgpu_timestep_host", "mifgpu_timestep_nhn",
     "mifgpu_timestep_velocity", "mifgpu_apply_bc", "mifgpu_solve_pressure", "mifgpu_divergence", "mifgpu_project",
     "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_profile_step", "mifgpu_launch_count",
-    "mifgpu_device_bytes",
+    "mifgpu_device_bytes", "mifgpu_gradient_ke", "mifgpu_backward", "mifgpu_download_adjoint",
+    "mifgpu_set_forcing_amplitude",
 ]
 PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
                    "x_inverse", "periodic", "project"]
@@ -94,6 +95,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_profile_step": [vp, d, i, dp],
         "mifgpu_launch_count": [vp, dp],
         "mifgpu_device_bytes": [vp, dp],
+        "mifgpu_gradient_ke": [vp, d, i, i, dp, dp, dp, dp],
+        "mifgpu_backward": [vp, d, i, i, dp, dp, dp, dp, dp, dp],
+        "mifgpu_download_adjoint": [vp, i, dp],
+        "mifgpu_set_forcing_amplitude": [vp, d],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -246,4 +251,53 @@ class Solver:
     def error_norms(self, t: float) -> np.ndarray:
         out = np.zeros(9)
         self._check(self.lib.mifgpu_error_norms(self.h, t, out.ctypes.data), "error_norms")
+        return out
+
+    # -- reverse mode (no counterpart in the reference) --
+    def set_forcing_amplitude(self, alpha: float) -> None:
+        self._check(self.lib.mifgpu_set_forcing_amplitude(self.h, float(alpha)), "set_forcing_amplitude")
+        self.params.forcing_amplitude = float(alpha)
+
+    def gradient_ke(self, t0: float, nsteps: int, checkpoint_every: int, box) -> dict:
+        """Kinetic energy in `box` (x0, x1, y0, y1, z0, z1) after `nsteps` steps from the
+        current state and its gradient; the state advances to the final time.
+
+        Returns loss, dloss_dalpha and the milliseconds of the forward pass, the
+        segment recomputes and the reverse sweeps; the gradients with respect to
+        the initial u, v, w, p come from ``adjoint(name)``."""
+        b = np.ascontiguousarray(box, dtype=np.float64)
+        loss, da = C.c_double(), C.c_double()
+        ms = np.zeros(3)
+        self._check(self.lib.mifgpu_gradient_ke(self.h, t0, int(nsteps), int(checkpoint_every), b.ctypes.data,
+                                                C.addressof(loss), C.addressof(da), ms.ctypes.data),
+                    "gradient_ke")
+        return {"loss": loss.value, "dloss_dalpha": da.value, "forward_ms": ms[0], "recompute_ms": ms[1],
+                "reverse_ms": ms[2]}
+
+    def backward(self, t0: float, nsteps: int, checkpoint_every: int, seeds: dict) -> dict:
+        """Back-propagates d loss / d (final u, v, w, p) (``seeds``, reference-layout arrays,
+        missing = 0) through `nsteps` steps from the current state."""
+        bufs = []
+        ptrs = []
+        for n in ("u", "v", "w", "p"):
+            if seeds.get(n) is None:
+                ptrs.append(None)
+                continue
+            a = np.ascontiguousarray(seeds[n], dtype=np.float64)
+            if a.shape != self.shape(n):
+                raise MifGpuError(f"seed {n}: shape {a.shape} != {self.shape(n)}")
+            bufs.append(a)
+            ptrs.append(a.ctypes.data)
+        da = C.c_double()
+        ms = np.zeros(3)
+        self._check(self.lib.mifgpu_backward(self.h, t0, int(nsteps), int(checkpoint_every), *ptrs,
+                                             C.addressof(da), ms.ctypes.data), "backward")
+        return {"dloss_dalpha": da.value, "forward_ms": ms[0], "recompute_ms": ms[1], "reverse_ms": ms[2]}
+
+    def adjoint(self, name: str) -> np.ndarray:
+        """d loss / d (initial field) of the last gradient_ke / backward call (u, v, w or p)."""
+        if name not in ("u", "v", "w", "p"):
+            raise MifGpuError(f"no adjoint field {name}")
+        out = np.empty(self.shape(name), dtype=np.float64)
+        self._check(self.lib.mifgpu_download_adjoint(self.h, FIELDS[name], out.ctypes.data), "download_adjoint")
         return out
