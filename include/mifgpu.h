@@ -217,6 +217,30 @@ int mifgpu_download_adjoint(mifgpu_ctx *ctx, int field, double *host);
 /* Changes alpha of the Taylor-Green forcing (re-captures the step graphs). */
 int mifgpu_set_forcing_amplitude(mifgpu_ctx *ctx, double alpha);
 
+/* Velocity error norms that allocate nothing. No counterpart in the
+ * reference: it is a variant of the velocity part of mifgpu_error_norms
+ * (out[0..2] = L1, L2, Linf of velocity set 0 against the boundary kind's
+ * exact velocity at t, src/Norms.cpp:11-47) for callers that cannot allocate
+ * device memory in the middle of a run: a time loop that has handed the rest
+ * of HBM to a caching allocator (PyTorch's, for one), where a lazy cudaMalloc
+ * fails with out-of-memory, and loops that cannot take the device-wide
+ * synchronisation cudaMalloc/cudaFree imply.
+ *
+ * Its partial sums live in one file-scope device array of the library
+ * (96 KB: 3 doubles for each of at most 4000 interior z planes, plus the
+ * totals); nothing in it has to start at zero, because every element the call
+ * reads it has written before. The reduction runs in a fixed order, so the
+ * result is bitwise reproducible. The call returns MIFGPU_EINVAL, with a
+ * message, for a z extent above 4002 points (more than 4000 interior
+ * planes), and when the context's device is not the current device. The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress)
+ * and caches it; make that first call before any stream capture begins on
+ * the device. The array is shared by every context on a device: calls whose
+ * executions overlap (other threads, other streams or contexts on the same
+ * device) race on it, so the caller serialises them. Returns after the three
+ * numbers have reached `out`. */
+int mifgpu_velocity_error_norms_noalloc(mifgpu_ctx *ctx, double t, double out[3]);
+
 /* Number of kernels this context has launched so far (for launch accounting). */
 int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out);
 

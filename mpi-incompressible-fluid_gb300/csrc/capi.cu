@@ -17,6 +17,7 @@
 #include "../../include/mifgpu.h"
 #include "adjoint_impl.cuh"
 #include "common.cuh"
+#include "noalloc.cuh"
 #include "poisson.cuh"
 #include "stencil.cuh"
 
@@ -921,6 +922,43 @@ int mifgpu_set_forcing_amplitude(mifgpu_ctx *ctx, double alpha) {
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->prm.forcing_amplitude = alpha;
   ctx->impl->drop_graphs();
+  return MIFGPU_OK;
+}
+
+int mifgpu_velocity_error_norms_noalloc(mifgpu_ctx *ctx, double t, double out[3]) {
+  if (!ctx || !out) return MIFGPU_EINVAL;
+  const Geometry &g = ctx->g;
+  const int planes = g.E[2] - 2;
+  if (planes > kNoAllocMaxPlanes)
+    return fail(ctx, MIFGPU_EINVAL,
+                "velocity_error_norms_noalloc: " + std::to_string(planes) + " interior z planes exceed the " +
+                    std::to_string(kNoAllocMaxPlanes) + " its static scratch holds (z extent at most " +
+                    std::to_string(kNoAllocMaxPlanes + 2) + ")");
+  int cur = -1;
+  CK(cudaGetDevice(&cur));
+  if (cur != ctx->device) return fail(ctx, MIFGPU_EINVAL, "velocity_error_norms_noalloc: the context's device is not current");
+  double *scratch = nullptr;
+  std::string err;
+  if (noalloc_scratch(&scratch, err)) return fail(ctx, MIFGPU_ECUDA, err);
+  const int kind = ctx->prm.boundary_kind;
+  if (ctx->prm.precision == MIFGPU_FP64)
+    launch_velocity_errors_noalloc<double>(g, (const double *)ctx->impl->field_ptr(0),
+                                           (const double *)ctx->impl->field_ptr(1),
+                                           (const double *)ctx->impl->field_ptr(2), kind, t, scratch, ctx->stream,
+                                           &ctx->launches);
+  else
+    launch_velocity_errors_noalloc<float>(g, (const float *)ctx->impl->field_ptr(0),
+                                          (const float *)ctx->impl->field_ptr(1),
+                                          (const float *)ctx->impl->field_ptr(2), kind, t, scratch, ctx->stream,
+                                          &ctx->launches);
+  CK(cudaGetLastError());
+  double h[3];
+  CK(cudaMemcpyAsync(h, scratch + 3 * kNoAllocMaxPlanes, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const double vol = g.h[0] * g.h[1] * g.h[2];
+  out[0] = h[0] * vol;
+  out[1] = std::sqrt(h[1] * vol);
+  out[2] = h[2];
   return MIFGPU_OK;
 }
 

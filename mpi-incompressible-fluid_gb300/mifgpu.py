@@ -34,7 +34,7 @@ EXPORTED = [
     "mifgpu_timestep_velocity", "mifgpu_apply_bc", "mifgpu_solve_pressure", "mifgpu_divergence", "mifgpu_project",
     "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_profile_step", "mifgpu_launch_count",
     "mifgpu_device_bytes", "mifgpu_gradient_ke", "mifgpu_backward", "mifgpu_download_adjoint",
-    "mifgpu_set_forcing_amplitude",
+    "mifgpu_set_forcing_amplitude", "mifgpu_velocity_error_norms_noalloc",
 ]
 PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
                    "x_inverse", "periodic", "project"]
@@ -99,6 +99,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_backward": [vp, d, i, i, dp, dp, dp, dp, dp, dp],
         "mifgpu_download_adjoint": [vp, i, dp],
         "mifgpu_set_forcing_amplitude": [vp, d],
+        "mifgpu_velocity_error_norms_noalloc": [vp, d, dp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -251,6 +252,14 @@ class Solver:
     def error_norms(self, t: float) -> np.ndarray:
         out = np.zeros(9)
         self._check(self.lib.mifgpu_error_norms(self.h, t, out.ctypes.data), "error_norms")
+        return out
+
+    def velocity_error_norms_noalloc(self, t: float) -> np.ndarray:
+        """L1, L2, Linf of the velocity error (error_norms()[0:3]) from a static
+        device scratch: no allocation, bitwise reproducible (see include/mifgpu.h)."""
+        out = np.zeros(3)
+        self._check(self.lib.mifgpu_velocity_error_norms_noalloc(self.h, t, out.ctypes.data),
+                    "velocity_error_norms_noalloc")
         return out
 
     # -- reverse mode (no counterpart in the reference) --

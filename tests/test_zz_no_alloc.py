@@ -1,0 +1,42 @@
+"""mifgpu_velocity_error_norms_noalloc: the velocity error norms from the
+library's static device scratch, compared with mifgpu_error_norms (the entry
+point that reduces into context memory) on two calls in a row. Collected last
+so that it also runs after every other GPU test of the session."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make(mg, n_global, precision, periodic=(False, False, False), kind=1):
+    return mg.Solver(n_global=n_global, Re=1000.0, dt=1e-4, periodic=periodic, precision=precision,
+                     boundary_kind=kind, forcing=mg.FORCING_NAVIER_STOKES)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_noalloc_norms_match_error_norms(mifgpu_lib, cuda_device, precision):
+    mg = mifgpu_lib
+    s = make(mg, (17, 18, 19), precision)
+    s.set_exact_velocity(0, 0.3)
+    s.set_exact_pressure(0.3)
+    rng = np.random.default_rng(2)
+    u = s.download("u")
+    s.upload("u", u + 1e-3 * rng.standard_normal(u.shape))
+    s.run(0.3, 2)
+    t = 0.3 + 2 * 1e-4
+    want = s.error_norms(t)[:3]
+    first = s.velocity_error_norms_noalloc(t)
+    second = s.velocity_error_norms_noalloc(t)
+    np.testing.assert_array_equal(first, second)  # fixed reduction order
+    np.testing.assert_allclose(first, want, rtol=1e-12, atol=0)
+    assert first[2] == want[2]  # the maximum does not depend on the order
+    s.close()
+
+
+def test_noalloc_norms_reject_too_many_planes(mifgpu_lib, cuda_device):
+    """A z extent of 4098 points (4096 interior planes) exceeds the 4000-plane scratch."""
+    mg = mifgpu_lib
+    s = make(mg, (5, 5, 4097), 0, periodic=(False, False, True), kind=0)
+    with pytest.raises(mg.MifGpuError, match="4000"):
+        s.velocity_error_norms_noalloc(0.0)
+    s.close()
