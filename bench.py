@@ -254,6 +254,25 @@ def random_solenoidal(shape_of, n, L, kmax, amp, seed):
     return out
 
 
+def ke_box(s, n, L, box):
+    """Kinetic energy 1/2 h^3 sum u_c^2 over the interior staggered points inside
+    box, for a periodic n^3 box of side L (the loss of mifgpu_gradient_ke)."""
+    import numpy as np
+
+    h = L / n
+    tot = 0.0
+    for c, nm in enumerate("uvw"):
+        a = s.download(nm)
+        ez, ey, ex = a.shape
+        ax = []
+        for d, e in enumerate((ex, ey, ez)):
+            x = h * (np.arange(e) - 1.0) - (h / 2 if d == c else 0.0)
+            ax.append((x >= box[2 * d]) & (x <= box[2 * d + 1]) & (np.arange(e) >= 1) & (np.arange(e) <= e - 2))
+        m = ax[2][:, None, None] & ax[1][None, :, None] & ax[0][None, None, :]
+        tot += 0.5 * h ** 3 * float(np.sum(a[m] ** 2))
+    return tot
+
+
 def adjoint_bench(stream):
     """Checkpointed gradient of the kinetic energy in [pi/2, 3pi/2]^3 after 200
     steps of a periodic 128^3 box, in FP32 and FP64: cost against the forward
@@ -303,17 +322,26 @@ def adjoint_bench(stream):
                                             (fwd_ms * a["nsteps"]), 3),
                "loss": r["loss"], "dloss_dalpha": r["dloss_dalpha"], "device_gb": round(s.device_bytes() / 1e9, 2)}
         if prec == mifgpu.FP64:
-            # dot-product test against the tangent-linear derivative (central difference)
+            # dot-product test: <adjoint, delta> against the tangent-linear derivative
+            # of the FP64 forward map along a random delta, by central differences at
+            # eps and eps/2 and their Richardson extrapolation (removes the eps^2 term)
             rng = np.random.default_rng(5)
             delta = {nm: rng.standard_normal(st[nm].shape) for nm in "uvw"}
             adj = sum(float(np.sum(g[nm] * delta[nm])) for nm in "uvw")
+
+            def loss_at(e):
+                s.load_state({nm: st[nm] + e * delta[nm] for nm in "uvw"} | {"p": st["p"]})
+                s.run(0.0, a["nsteps"])
+                return ke_box(s, n, a["L"], box)
+
             eps = 1e-6
-            ls = []
-            for sign in (1, -1):
-                s.load_state({nm: st[nm] + sign * eps * delta[nm] for nm in "uvw"} | {"p": st["p"]})
-                ls.append(s.gradient_ke(0.0, a["nsteps"], a["every"], box)["loss"])
-            tl = (ls[0] - ls[1]) / (2 * eps)
-            out["dot_product_rel_err"] = abs(tl - adj) / abs(tl)
+            d1 = (loss_at(eps) - loss_at(-eps)) / (2 * eps)
+            d2 = (loss_at(eps / 2) - loss_at(-eps / 2)) / eps
+            dr = (4 * d2 - d1) / 3
+            out["dot_product"] = {"adjoint": adj, "tangent_linear_eps": d1, "tangent_linear_eps_half": d2,
+                                  "eps": eps, "rel_err_eps": abs(d1 - adj) / abs(adj),
+                                  "rel_err_eps_half": abs(d2 - adj) / abs(adj),
+                                  "rel_err_richardson": abs(dr - adj) / abs(adj)}
         res[prec_name] = out
         s.close()
         torch.cuda.empty_cache()

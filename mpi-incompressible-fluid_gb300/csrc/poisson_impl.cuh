@@ -22,6 +22,8 @@
 // inverse transform, so the spectrum along z never leaves shared memory.
 #pragma once
 
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <type_traits>
@@ -652,6 +654,19 @@ void AxisPlan<T>::release() {
   lam_dev = nullptr;
 }
 
+// The dynamic shared-memory limit is an attribute of the kernel, shared by
+// every solver of the process: raise it to what this solver needs, never lower
+// it below what an earlier (still live) solver set.
+inline cudaError_t raise_dynamic_smem(const void *fn, size_t bytes) {
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+  if (e != cudaSuccess) return e;
+  if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 template <typename T>
 int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
   geo = g;
@@ -678,8 +693,7 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
     if (!axis[d].reg_n1) continue;
     for (int mode = 0; mode < 3; ++mode) {
       const void *fn = RegKernels<T>::get(axis[d].reg_n1, axis[d].reg_n2, mode, axis[d].kind);
-      if (!fn || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)axis[d].reg_smem) !=
-                     cudaSuccess) {
+      if (!fn || raise_dynamic_smem(fn, axis[d].reg_smem) != cudaSuccess) {
         err = "register-path kernel set-up failed";
         return -2;
       }
@@ -690,7 +704,7 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
     const void *fn = mode == 0   ? (const void *)line_kernel<T, kModeForward>
                      : mode == 1 ? (const void *)line_kernel<T, kModeInverse>
                                  : (const void *)line_kernel<T, kModeFwdEigInv>;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max) != cudaSuccess) {
+    if (raise_dynamic_smem(fn, smem_max) != cudaSuccess) {
       err = "cudaFuncSetAttribute(MaxDynamicSharedMemorySize) failed";
       return -2;
     }

@@ -115,6 +115,22 @@ def test_fp64_steps_match_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, per
         assert field_err(n, g.download(n), o.get(n), o.get("p")) <= FP64_TOL, n
 
 
+def test_contexts_of_different_sizes_coexist(oracle_lib, mifgpu_lib, cuda_device):
+    """A context whose line kernels need more dynamic shared memory keeps
+    working after a smaller context was created (the kernel attribute is
+    process-wide and only ever raised)."""
+    kw = dict(n_global=(17, 18, 257), size=(1.0, 1.0, 2.0), Re=500.0, dt=1e-4, exact_kind=2)
+    o, big = _oracle_pair(oracle_lib, mifgpu_lib, kw)
+    small = make_solver(mifgpu_lib, dict(n_global=(9, 9, 9), exact_kind=2))
+    small.set_exact_velocity(0, 0.0)
+    small.run(0.0, 1)
+    big.run(0.0, 2)
+    for k in range(2):
+        o.timestep(k * kw["dt"])
+    for n in oracle_lib.FIELD_NAMES:
+        assert field_err(n, big.download(n), o.get(n), o.get("p")) <= FP64_TOL, n
+
+
 def test_forcing_extension_matches_oracle(oracle_lib, mifgpu_lib, cuda_device):
     """Projection step with the SINCOS Navier-Stokes forcing (the labelled
     extension for manufactured-solution runs)."""
