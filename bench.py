@@ -543,11 +543,21 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="only the adjoint workload (a profiling aid; prints {'adjoint': ...})")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.adjoint_only:
+        import torch
+
+        import build as pkg_build
+
+        pkg_build.build()
+        stream = torch.cuda.Stream()
+        print(json.dumps({"adjoint": adjoint_bench(stream)}))
     else:
         run_gpu(args)
 

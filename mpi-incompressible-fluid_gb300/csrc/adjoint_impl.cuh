@@ -1,16 +1,17 @@
 // Discrete adjoint of the projection step (sm_103a): the transposes of every
 // linear map of src/Timestep.cpp:97-141 and of the linearised momentum
 // right-hand side of include/MomentumEquation.h:42-255, as gather kernels
-// (one thread per output point, no atomics on fields, deterministic).
+// (one thread per output point, no atomics, deterministic).
 //
 // The reference has no adjoint; this is an extension. Notation:
 //   R_c(P)  momentum right-hand side of component c at its interior point P
 //   G       one-sided pressure gradient onto interior velocity points
 //   D       divergence at the pressure owner points
 //   M       the spectral Poisson solve on the owner block
-// Adjoint weights of R_c are zero outside the interior of component c, so
-// every gather masks its reads with the interior predicate; that also keeps
-// every state read inside the field.
+// Adjoint weights of R_c are zero outside the interior of component c; the
+// split kernel stores them so, and the gathers rely on it instead of masking
+// each read. Reductions (the loss, d loss / d alpha) go through per-block
+// partial sums added in a fixed order, so results are bitwise reproducible.
 //
 // M is not symmetric on a Neumann (DCT-I) axis: the reflection closure of
 // the Laplacian there is symmetric only in the trapezoid inner product with
@@ -28,6 +29,20 @@
 namespace mifgpu {
 
 namespace adj {
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem_adj(T *smem, const T *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_commit_adj() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait_adj() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
 
 __device__ __forceinline__ bool interior(const Geometry &g, int c, long i, long j, long k) {
   return i >= 1 && j >= 1 && k >= 1 && i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
@@ -49,89 +64,147 @@ __device__ __forceinline__ double trap_weight(const Geometry &g, long i, long j,
   return w;
 }
 
+// ---- transposed momentum right-hand side, shared-memory tiled ----
+//
+// A CTA owns a TX x TY tile of (i, j) and marches through kc planes of k,
+// like the forward stage kernel. The three adjoint weights mu_c and the three
+// linearisation fields V_c live in a ring of six shared-memory planes per
+// field (k-2 .. k+2 and the plane being prefetched), each with a two-point
+// halo in x and y: the gather reads V up to two points away along one axis
+// (Avg_{d,c} at P = Q + e_d, and the cross terms at P = Q - e_f). mu is zero
+// off the interior of its component in memory (the split kernel writes those
+// zeros and the padding is cleared once), so no read needs a mask.
+constexpr int kATX = 32, kATY = 8, kAH = 2;
+constexpr int kAHX = kATX + 2 * kAH, kAHY = kATY + 2 * kAH, kAPL = kAHX * kAHY;
+constexpr int kASlots = 6;
+
 template <typename T>
-struct View {
-  Geometry g;
-  const T *mu[3];  // adjoint weights of R_c
-  const T *V[3];   // state R was linearised at
-  __device__ __forceinline__ T M(int c, long i, long j, long k) const {
-    return interior(g, c, i, j, k) ? mu[c][g.idx(i, j, k)] : T(0);
-  }
-  __device__ __forceinline__ T S(int c, long i, long j, long k) const { return V[c][g.idx(i, j, k)]; }
+struct AdjRing {
+  T f[6][kASlots][kAPL];  // mu_u, mu_v, mu_w, V_u, V_v, V_w; slot (k mod 6); tile
 };
 
-// Avg_{d,c}(P) = V_d(P) + V_d(P+e_d) + V_d(P-e_c) + V_d(P-e_c+e_d): the four
-// V_d values the convection of component c averages (d != c).
 template <typename T>
-__device__ __forceinline__ T avg_dc(const View<T> &A, int d, int c, long i, long j, long k) {
-  const long di = d == 0, dj = d == 1, dk = d == 2;
-  const long ci = c == 0, cj = c == 1, ck = c == 2;
-  return A.S(d, i, j, k) + A.S(d, i + di, j + dj, k + dk) + A.S(d, i - ci, j - cj, k - ck) +
-         A.S(d, i - ci + di, j - cj + dj, k - ck + dk);
+struct ATap {
+  const AdjRing<T> *r;
+  int base;      // (ty + kAH) * kAHX + tx + kAH
+  int slot[5];   // slot of plane k + dk for dk = -2 .. 2
+  __device__ __forceinline__ T mu(int c, int di, int dj, int dk) const {
+    return r->f[c][slot[dk + 2]][base + dj * kAHX + di];
+  }
+  __device__ __forceinline__ T v(int c, int di, int dj, int dk) const {
+    return r->f[3 + c][slot[dk + 2]][base + dj * kAHX + di];
+  }
+};
+
+// Avg_{d,c}(P) = V_d(P) + V_d(P+e_d) + V_d(P-e_c) + V_d(P-e_c+e_d) at P = Q + (a, b, e).
+template <typename T, int D, int C>
+__device__ __forceinline__ T avg_tap(const ATap<T> &A, int a, int b, int e) {
+  constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+  constexpr int ci = C == 0, cj = C == 1, ck = C == 2;
+  return A.v(D, a, b, e) + A.v(D, a + di, b + dj, e + dk) + A.v(D, a - ci, b - cj, e - ck) +
+         A.v(D, a - ci + di, b - cj + dj, e - ck + dk);
 }
 
-// (R'(V)^T mu)_f at Q = (i, j, k), with
+// Cross term of R_C read through Avg_{F,C}: sum over P in {Q, Q-e_F, Q+e_C, Q+e_C-e_F}
+// of mu_C(P) (V_C(P+e_F) - V_C(P-e_F)) o8h_F.
+template <typename T, int F, int C>
+__device__ __forceinline__ T cross_tap(const ATap<T> &A) {
+  constexpr int fi = F == 0, fj = F == 1, fk = F == 2;
+  constexpr int ci = C == 0, cj = C == 1, ck = C == 2;
+  T s = T(0);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int a = (r >= 2 ? ci : 0) - (r & 1 ? fi : 0);
+    const int b = (r >= 2 ? cj : 0) - (r & 1 ? fj : 0);
+    const int e = (r >= 2 ? ck : 0) - (r & 1 ? fk : 0);
+    s += A.mu(C, a, b, e) * (A.v(C, a + fi, b + fj, e + fk) - A.v(C, a - fi, b - fj, e - fk));
+  }
+  return s;
+}
+
+// Self-convection of R_F by V_D (D != F): mu_F(Q-e_D) Avg_{D,F}(Q-e_D) - mu_F(Q+e_D) Avg_{D,F}(Q+e_D).
+template <typename T, int F, int D>
+__device__ __forceinline__ T conv_tap(const ATap<T> &A) {
+  constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+  return A.mu(F, -di, -dj, -dk) * avg_tap<T, D, F>(A, -di, -dj, -dk) -
+         A.mu(F, di, dj, dk) * avg_tap<T, D, F>(A, di, dj, dk);
+}
+
+// (R'(V)^T mu)_F at the tap's point, with
 //   R_c(P) = - V_c(P) (V_c(P+e_c) - V_c(P-e_c)) o2h_c
 //            - sum_{d != c} Avg_{d,c}(P) (V_c(P+e_d) - V_c(P-e_d)) o8h_d
 //            + sum_d (V_c(P+e_d) - 2 V_c(P) + V_c(P-e_d)) oh2Re_d
-template <typename T>
-__device__ T rhs_adjoint_point(const View<T> &A, const Coeffs<T> &co, int f, long i, long j, long k) {
-  T acc = T(0);
-  {
-    const int c = f;
-    const long ei = c == 0, ej = c == 1, ek = c == 2;
-    const T m0 = A.M(c, i, j, k);
-    if (m0 != T(0)) acc -= m0 * (A.S(c, i + ei, j + ej, k + ek) - A.S(c, i - ei, j - ej, k - ek)) * co.o2h[c];
-    const T mm = A.M(c, i - ei, j - ej, k - ek);
-    if (mm != T(0)) acc -= mm * A.S(c, i - ei, j - ej, k - ek) * co.o2h[c];
-    const T mp = A.M(c, i + ei, j + ej, k + ek);
-    if (mp != T(0)) acc += mp * A.S(c, i + ei, j + ej, k + ek) * co.o2h[c];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const long di = d == 0, dj = d == 1, dk = d == 2;
-      const T mdm = A.M(c, i - di, j - dj, k - dk);
-      const T mdp = A.M(c, i + di, j + dj, k + dk);
-      if (d != c) {
-        if (mdm != T(0)) acc -= mdm * avg_dc(A, d, c, i - di, j - dj, k - dk) * co.o8h[d];
-        if (mdp != T(0)) acc += mdp * avg_dc(A, d, c, i + di, j + dj, k + dk) * co.o8h[d];
-      }
-      acc += (mdp - T(2) * m0 + mdm) * co.oh2Re[d];
-    }
-  }
-  // R_c for c != f reads V_f through Avg_{f,c}(P) at P in {Q, Q-e_f, Q+e_c, Q+e_c-e_f}.
-  const long di = f == 0, dj = f == 1, dk = f == 2;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    if (c == f) continue;
-    const long ci = c == 0, cj = c == 1, ck = c == 2;
-    const long P[4][3] = {{i, j, k},
-                          {i - di, j - dj, k - dk},
-                          {i + ci, j + cj, k + ck},
-                          {i + ci - di, j + cj - dj, k + ck - dk}};
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const T m = A.M(c, P[r][0], P[r][1], P[r][2]);
-      if (m == T(0)) continue;
-      const T dv = A.S(c, P[r][0] + di, P[r][1] + dj, P[r][2] + dk) - A.S(c, P[r][0] - di, P[r][1] - dj, P[r][2] - dk);
-      acc -= m * dv * co.o8h[f];
-    }
-  }
+template <typename T, int F>
+__device__ __forceinline__ T rhs_adjoint_tap(const ATap<T> &A, const Coeffs<T> &co) {
+  constexpr int fi = F == 0, fj = F == 1, fk = F == 2;
+  constexpr int D1 = F == 0 ? 1 : 0, D2 = F == 2 ? 1 : 2;  // the two other axes
+  const T m0 = A.mu(F, 0, 0, 0);
+  const T mm = A.mu(F, -fi, -fj, -fk), mp = A.mu(F, fi, fj, fk);
+  // self-advection along F
+  T acc = (mp * A.v(F, fi, fj, fk) - mm * A.v(F, -fi, -fj, -fk) -
+           m0 * (A.v(F, fi, fj, fk) - A.v(F, -fi, -fj, -fk))) * co.o2h[F];
+  // convection of F by the other two components
+  acc -= conv_tap<T, F, D1>(A) * co.o8h[D1];
+  acc -= conv_tap<T, F, D2>(A) * co.o8h[D2];
+  // diffusion
+  acc += (mp - T(2) * m0 + mm) * co.oh2Re[F];
+  acc += (A.mu(F, D1 == 0, D1 == 1, D1 == 2) - T(2) * m0 + A.mu(F, -(D1 == 0), -(D1 == 1), -(D1 == 2))) *
+         co.oh2Re[D1];
+  acc += (A.mu(F, D2 == 0, D2 == 1, D2 == 2) - T(2) * m0 + A.mu(F, -(D2 == 0), -(D2 == 1), -(D2 == 2))) *
+         co.oh2Re[D2];
+  // the other components' convection reads V_F through their averages
+  acc -= (cross_tap<T, F, D1>(A) + cross_tap<T, F, D2>(A)) * co.o8h[F];
   return acc;
 }
 
-// lam_f += (R'(V)^T mu)_f on every point of the three fields.
+// lam_c += (R'(V)^T mu)_c on every point of the three fields.
 template <typename T>
-__global__ void rhs_adjoint_kernel(View<T> A, Coeffs<T> co, T *l0, T *l1, T *l2) {
-  const long i = blockIdx.x * blockDim.x + threadIdx.x;
-  const long j = blockIdx.y * blockDim.y + threadIdx.y;
-  const long k = blockIdx.z;
+__global__ void __launch_bounds__(kATX *kATY) rhs_adjoint_tiled(Geometry g, Coeffs<T> co, const T *m0, const T *m1,
+                                                                const T *m2, const T *v0, const T *v1, const T *v2,
+                                                                T *l0, T *l1, T *l2, int kc) {
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  AdjRing<T> &ring = *reinterpret_cast<AdjRing<T> *>(adj_smem);
+  const T *src[6] = {m0, m1, m2, v0, v1, v2};
+  const int tx = threadIdx.x % kATX, ty = threadIdx.x / kATX;
+  const int i0 = blockIdx.x * kATX, j0 = blockIdx.y * kATY;
+  const int kbeg = blockIdx.z * kc, kend = min(kbeg + kc, g.Es[2]);
+  auto load_plane = [&](int kk) {
+    const int sl = (kk + 2 * kASlots) % kASlots;
+    for (int e = threadIdx.x; e < kAPL; e += kATX * kATY) {
+      const int hx = e % kAHX, hy = e / kAHX;
+      const int i = i0 - kAH + hx, j = j0 - kAH + hy;
+      const bool ok = kk >= 0 && kk < g.PZ && i >= 0 && i < g.PX && j >= 0 && j < g.PY;
+      const long q = ok ? g.idx(i, j, kk) : 0;
+#pragma unroll
+      for (int f = 0; f < 6; ++f) {
+        T *d = &ring.f[f][sl][e];
+        if (ok)
+          cp_async_elem_adj(d, src[f] + q);
+        else
+          *d = T(0);
+      }
+    }
+    cp_commit_adj();
+  };
+  for (int kk = kbeg - 2; kk <= kbeg + 2; ++kk) load_plane(kk);
+  const int i = i0 + tx, j = j0 + ty;
   T *lam[3] = {l0, l1, l2};
-  const long q = A.g.idx(i, j, k);
-#pragma unroll 1
-  for (int f = 0; f < 3; ++f) {
-    if (i >= A.g.ext(f, 0) || j >= A.g.ext(f, 1) || k >= A.g.ext(f, 2)) continue;
-    lam[f][q] += rhs_adjoint_point(A, co, f, i, j, k);
+  ATap<T> A;
+  A.r = &ring;
+  A.base = (ty + kAH) * kAHX + tx + kAH;
+  for (int k = kbeg; k < kend; ++k) {
+    load_plane(k + 3);
+    cp_wait_adj<1>();
+    __syncthreads();
+#pragma unroll
+    for (int dk = -2; dk <= 2; ++dk) A.slot[dk + 2] = (k + dk + 2 * kASlots) % kASlots;
+    const long q = g.idx(i, j, k);
+    if (i < g.ext(0, 0) && j < g.ext(0, 1) && k < g.ext(0, 2)) lam[0][q] += rhs_adjoint_tap<T, 0>(A, co);
+    if (i < g.ext(1, 0) && j < g.ext(1, 1) && k < g.ext(1, 2)) lam[1][q] += rhs_adjoint_tap<T, 1>(A, co);
+    if (i < g.ext(2, 0) && j < g.ext(2, 1) && k < g.ext(2, 2)) lam[2][q] += rhs_adjoint_tap<T, 2>(A, co);
+    __syncthreads();  // the next iteration refills the slot of plane k - 2
   }
+  cp_wait_adj<0>();
 }
 
 // out(r) = (add(r) + scale (G^T mu)(r)) / (weighted ? W(r) : 1) on the pressure
@@ -230,15 +303,46 @@ __global__ void dirichlet_adjoint_kernel(Geometry g, T *f0, T *f1, T *f2) {
   }
 }
 
+// Sum of v over the block (32 x 8 threads) in a fixed order, written to
+// part[linear block index] by thread 0: deterministic partial sums.
+__device__ __forceinline__ void block_partial(double v, double *part) {
+  __shared__ double w[8];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  if ((t & 31) == 0) w[t >> 5] = v;
+  __syncthreads();
+  if (t == 0) {
+    double s = 0.0;
+    for (int q = 0; q < 8; ++q) s += w[q];
+    part[blockIdx.x + (long)gridDim.x * (blockIdx.y + (long)gridDim.y * blockIdx.z)] = s;
+  }
+}
+
+// *out (+)= sum of part[0 .. n) in a fixed order (one block of 256 threads).
+__global__ void sum_partials_kernel(const double *part, long n, double *out, int accumulate) {
+  __shared__ double w[256];
+  double v = 0.0;
+  for (long q = threadIdx.x; q < n; q += 256) v += part[q];
+  w[threadIdx.x] = v;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) w[threadIdx.x] += w[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = accumulate ? *out + w[0] : w[0];
+}
+
 // Split of the adjoint of one stage's pre-projection set X (lx, zero off the
 // interior) on the interior points:
 //   mu   = a lx + b pend      (adjoint weights of this stage's R)
 //   pend = a2 lx              (when write_pend: the share of an earlier R)
-// and, when tab is given, acc += sum mu_c F_c with F the Taylor-Green
-// body-force pattern (sin x cos y cos z, -cos x sin y cos z, 0).
+// mu is written as 0 on the other points of each component's extents (the
+// tiled gather relies on it). When tab is given, each block writes its share
+// of sum mu_c F_c to part[], F the Taylor-Green body-force pattern
+// (sin x cos y cos z, -cos x sin y cos z, 0).
 template <typename T>
 __global__ void split_kernel(Geometry g, T *m0, T *m1, T *m2, T *p0, T *p1, T *p2, const T *x0, const T *x1,
-                             const T *x2, T a, T b, T a2, int write_pend, const T *tab, int maxE, double *acc) {
+                             const T *x2, T a, T b, T a2, int write_pend, const T *tab, int maxE, double *part) {
   const long i = blockIdx.x * blockDim.x + threadIdx.x;
   const long j = blockIdx.y * blockDim.y + threadIdx.y;
   const long k = blockIdx.z;
@@ -248,7 +352,11 @@ __global__ void split_kernel(Geometry g, T *m0, T *m1, T *m2, T *p0, T *p1, T *p
   double f = 0.0;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    if (!interior(g, c, i, j, k)) continue;
+    if (i >= g.ext(c, 0) || j >= g.ext(c, 1) || k >= g.ext(c, 2)) continue;
+    if (!interior(g, c, i, j, k)) {
+      mu[c][q] = T(0);
+      continue;
+    }
     const T x = lx[c][q];
     T m = a * x;
     if (b != T(0)) m += b * pend[c][q];
@@ -263,17 +371,16 @@ __global__ void split_kernel(Geometry g, T *m0, T *m1, T *m2, T *p0, T *p1, T *p
         f -= (double)m * (C(0, 0, i) * S(1, 1, j) * C(2, 0, k));
     }
   }
-  if (!tab) return;
-  for (int o = 16; o > 0; o >>= 1) f += __shfl_down_sync(0xffffffffu, f, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(acc, f);
+  if (tab) block_partial(f, part);
 }
 
 // Kinetic energy in an axis-aligned box at the staggered points:
 //   L = 1/2 vol sum_c sum_{q interior of c, position in box} u_c(q)^2
-// lam_c(q) = vol u_c(q) there and 0 on every other point; acc += L.
+// lam_c(q) = vol u_c(q) there and 0 on every other point; each block writes
+// its share of L to part[].
 template <typename T>
 __global__ void ke_seed_kernel(Geometry g, const T *u0, const T *u1, const T *u2, T *l0, T *l1, T *l2, double x0,
-                               double x1, double y0, double y1, double z0, double z1, double *acc) {
+                               double x1, double y0, double y1, double z0, double z1, double *part) {
   const long i = blockIdx.x * blockDim.x + threadIdx.x;
   const long j = blockIdx.y * blockDim.y + threadIdx.y;
   const long k = blockIdx.z;
@@ -293,8 +400,7 @@ __global__ void ke_seed_kernel(Geometry g, const T *u0, const T *u1, const T *u2
     l[c][q] = in ? T(vol * v) : T(0);
     if (in) a += 0.5 * vol * v * v;
   }
-  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(acc, a);
+  block_partial(a, part);
 }
 
 inline unsigned cdiv_u(long a, long b) { return (unsigned)((a + b - 1) / b); }
@@ -319,10 +425,19 @@ struct AdjointOps {
     }
     return co;
   }
+  // Kernel attributes; call once before the first launch (outside stream capture).
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(adj::rhs_adjoint_tiled<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(adj::AdjRing<T>));
+  }
+  // Needs mu zero off each component's interior, padding included, and prepare().
   static void rhs_adjoint(const Geometry &g, T *const lam[3], const T *const mu[3], const T *const V[3],
                           cudaStream_t s, long long *cnt) {
-    adj::View<T> A{g, {mu[0], mu[1], mu[2]}, {V[0], V[1], V[2]}};
-    adj::rhs_adjoint_kernel<T><<<box_grid(g), dim3(32, 8), 0, s>>>(A, coeffs(g), lam[0], lam[1], lam[2]);
+    const int nx = std::max(g.Es[0], g.E[0]);
+    const int kc = g.Es[2] >= 256 ? 32 : 16;
+    const dim3 grid(adj::cdiv_u(nx, adj::kATX), adj::cdiv_u(g.Es[1], adj::kATY), adj::cdiv_u(g.Es[2], kc));
+    adj::rhs_adjoint_tiled<T><<<grid, adj::kATX * adj::kATY, sizeof(adj::AdjRing<T>), s>>>(
+        g, coeffs(g), mu[0], mu[1], mu[2], V[0], V[1], V[2], lam[0], lam[1], lam[2], kc);
     ++*cnt;
   }
   static void grad_adjoint(const Geometry &g, T *out, const T *add, const T *const mu[3], double scale,
@@ -364,19 +479,31 @@ struct AdjointOps {
       ++*cnt;
     }
   }
+  // Blocks of box_grid: the length of the partial-sum array.
+  static long box_blocks(const Geometry &g) {
+    const dim3 b = box_grid(g);
+    return (long)b.x * b.y * b.z;
+  }
+  // With tab: *acc += sum mu . F, through part[box_blocks] in a fixed order.
   static void split(const Geometry &g, T *const mu[3], T *const pend[3], const T *const lx[3], double a, double b,
-                    double a2, bool write_pend, const T *tab, int maxE, double *acc, cudaStream_t s,
+                    double a2, bool write_pend, const T *tab, int maxE, double *part, double *acc, cudaStream_t s,
                     long long *cnt) {
     adj::split_kernel<T><<<box_grid(g), dim3(32, 8), 0, s>>>(g, mu[0], mu[1], mu[2], pend[0], pend[1], pend[2],
                                                              lx[0], lx[1], lx[2], T(a), T(b), T(a2),
-                                                             write_pend ? 1 : 0, tab, maxE, acc);
+                                                             write_pend ? 1 : 0, tab, maxE, part);
     ++*cnt;
+    if (tab) {
+      adj::sum_partials_kernel<<<1, 256, 0, s>>>(part, box_blocks(g), acc, 1);
+      ++*cnt;
+    }
   }
-  static void ke_seed(const Geometry &g, const T *const u[3], T *const lam[3], const double box[6], double *acc,
-                      cudaStream_t s, long long *cnt) {
+  // *acc = the loss, through part[box_blocks].
+  static void ke_seed(const Geometry &g, const T *const u[3], T *const lam[3], const double box[6], double *part,
+                      double *acc, cudaStream_t s, long long *cnt) {
     adj::ke_seed_kernel<T><<<box_grid(g), dim3(32, 8), 0, s>>>(g, u[0], u[1], u[2], lam[0], lam[1], lam[2], box[0],
-                                                               box[1], box[2], box[3], box[4], box[5], acc);
-    ++*cnt;
+                                                               box[1], box[2], box[3], box[4], box[5], part);
+    adj::sum_partials_kernel<<<1, 256, 0, s>>>(part, box_blocks(g), acc, 0);
+    *cnt += 2;
   }
 };
 

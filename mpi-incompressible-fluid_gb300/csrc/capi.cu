@@ -172,6 +172,10 @@ struct Impl final : ImplBase {
   size_t ckpt_fields = 0;
   T *snap_block = nullptr;
   size_t snap_fields = 0;
+  double *red_part = nullptr;  // per-block partial sums of the adjoint reductions
+  // One captured reverse step per snapshot slot (the slot's address is baked in).
+  std::vector<cudaGraphExec_t> rev_graph;
+  long long rev_graph_launches = 0;
 
   void mark(int cls, cudaStream_t s) {
     if (!prof) return;
@@ -196,6 +200,9 @@ struct Impl final : ImplBase {
     cudaFree(adj_block);
     cudaFree(ckpt_block);
     cudaFree(snap_block);
+    cudaFree(red_part);
+    for (auto &gx : rev_graph)
+      if (gx) cudaGraphExecDestroy(gx);
     if (cap_stream) cudaStreamDestroy(cap_stream);
   }
 
@@ -544,9 +551,32 @@ struct Impl final : ImplBase {
       // X = prev + a_own R(prev) + a_prev R_prev - b_p G p on the interior
       Ops::grad_adjoint(g, lp, lp, lx, -b_p[st], false, s, cnt);
       Ops::split(g, mu, pend, lx, a_own[st], st < 2 ? 1.0 : 0.0, a_prev[st], st > 0, tg ? ftab : nullptr, ftab_maxE,
-                 dalpha, s, cnt);
+                 red_part, dalpha, s, cnt);
       Ops::rhs_adjoint(g, lx, mu, V[st], s, cnt);
     }
+  }
+
+  // The reverse step of snapshot slot m as a graph, captured on first use.
+  int ensure_rev_graph(mifgpu_ctx *ctx, int m, const T *const V[3][3]) {
+    if ((int)rev_graph.size() <= m) rev_graph.resize(m + 1, nullptr);
+    if (rev_graph[m]) return MIFGPU_OK;
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+    long long n = 0;
+    reverse_step(ctx, cap_stream, V, acc + 1, &n);
+    cudaError_t e = cudaStreamEndCapture(cap_stream, &gr);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream capture of the reverse step");
+    e = cudaGraphInstantiate(&rev_graph[m], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate (reverse step)");
+    rev_graph_launches = n;
+    return MIFGPU_OK;
+  }
+
+  void drop_rev_graphs() {
+    for (auto &gx : rev_graph)
+      if (gx) cudaGraphExecDestroy(gx);
+    rev_graph.clear();
   }
 
   int gradient(mifgpu_ctx *ctx, const GradRequest &req) override {
@@ -554,10 +584,24 @@ struct Impl final : ImplBase {
     const int C = std::max(1, std::min(req.every, N));
     if (C > slots_cap) return fail(ctx, MIFGPU_EINVAL, "checkpoint interval above 1024 steps");
     const int nseg = (N + C - 1) / C;
-    size_t have_adj = adj_block ? (size_t)kAdjFields : 0;
-    if (int rc = ensure_fields(ctx, adj_block, have_adj, kAdjFields, "adjoint fields")) return rc;
+    if (!adj_block) {
+      size_t have_adj = 0;
+      if (int rc = ensure_fields(ctx, adj_block, have_adj, kAdjFields, "adjoint fields")) return rc;
+      // mu must read 0 off the interior, padding included (the split kernel
+      // never writes the padding)
+      CK(cudaMemset(adj_block, 0, sizeof(T) * field_elems * kAdjFields));
+      const long nb = AdjointOps<T>::box_blocks(g);
+      if (cudaMalloc(&red_part, sizeof(double) * nb) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the adjoint partial sums failed");
+      }
+      total_bytes += sizeof(double) * nb;
+      CK(AdjointOps<T>::prepare());
+    }
     if (int rc = ensure_fields(ctx, ckpt_block, ckpt_fields, (size_t)4 * (nseg + 1), "checkpoints")) return rc;
+    T *const snap_before = snap_block;
     if (int rc = ensure_fields(ctx, snap_block, snap_fields, (size_t)9 * C, "segment snapshots")) return rc;
+    if (snap_block != snap_before) drop_rev_graphs();
     if (int rc = ensure_graph(ctx, kVariantProjection)) return rc;
     cudaStream_t s = ctx->stream;
     long long *cnt = &ctx->launches;
@@ -606,10 +650,11 @@ struct Impl final : ImplBase {
     CK(cudaMemsetAsync(acc, 0, sizeof(double) * 2, s));
     if (req.box) {
       const T *u[3] = {set0, set0 + field_elems, set0 + 2 * field_elems};
-      AdjointOps<T>::ke_seed(g, u, lx, req.box, acc, s, cnt);
+      AdjointOps<T>::ke_seed(g, u, lx, req.box, red_part, acc, s, cnt);
       CK(cudaMemsetAsync(adj_field(kLP), 0, sizeof(T) * field_elems, s));
     } else {
-      CK(cudaMemsetAsync(adj_block, 0, sizeof(T) * field_elems * kAdjFields, s));
+      for (int q = 0; q < 3; ++q) CK(cudaMemsetAsync(lx[q], 0, sizeof(T) * field_elems, s));
+      CK(cudaMemsetAsync(adj_field(kLP), 0, sizeof(T) * field_elems, s));
       if (int rc = ensure_staging(ctx)) return cleanup(), rc;
       const int ids[4] = {0, 1, 2, kP};
       T *dst[4] = {lx[0], lx[1], lx[2], adj_field(kLP)};
@@ -635,7 +680,9 @@ struct Impl final : ImplBase {
         const T *V[3][3];
         for (int st = 0; st < 3; ++st)
           for (int c = 0; c < 3; ++c) V[st][c] = sn(m) + (size_t)(3 * st + c) * field_elems;
-        reverse_step(ctx, s, V, acc + 1, cnt);
+        if (int rc = ensure_rev_graph(ctx, m, V)) return cleanup(), rc;
+        CK(cudaGraphLaunch(rev_graph[m], s));
+        *cnt += rev_graph_launches;
       }
     }
     phase(3);
@@ -676,6 +723,7 @@ struct Impl final : ImplBase {
 
   // Captured graphs hold the stage scalars: drop them when one changes.
   void drop_graphs() override {
+    drop_rev_graphs();
     for (auto &gv : graph)
       for (auto &gx : gv)
         if (gx) {

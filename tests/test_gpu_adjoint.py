@@ -10,7 +10,8 @@ gradient is checked against the library's own forward map, in FP64, by
   * the dot-product test: <adjoint, delta> against the tangent-linear
     derivative of the loss along a random delta (central difference,
     eps = 1e-6),
-  * the derivative with respect to the Taylor-Green forcing amplitude,
+  * the derivative with respect to the Taylor-Green forcing amplitude
+    (step 1e-4),
 each to a relative error of 1e-6 (the benchmark spec's bound), on a periodic box,
 an all-Dirichlet box with time-dependent wall data and a channel. The FP32
 adjoint is compared with the FP64 one; the checkpoint interval must not
@@ -190,7 +191,9 @@ def test_forcing_amplitude_derivative(fp64_runs, name):
     s, st, r, g = fp64_runs[name]
     c = CASES[name]
     a = c["alpha"]
-    fd = (loss_only(s, c, st, a + EPS) - loss_only(s, c, st, a - EPS)) / (2 * EPS)
+    # alpha moves the loss by as little as 1e-6 per unit on the short wall case:
+    # the larger step keeps the difference clear of the loss's last bits
+    fd = (loss_only(s, c, st, a + EPS_POINT) - loss_only(s, c, st, a - EPS_POINT)) / (2 * EPS_POINT)
     err = abs(fd - r["dloss_dalpha"]) / abs(fd)
     print(f"{name}: dL/dalpha fd {fd:.12e} adjoint {r['dloss_dalpha']:.12e} rel {err:.2e}")
     assert err <= TOL
@@ -201,10 +204,10 @@ def test_checkpoint_interval_does_not_change_gradient(fp64_runs):
     c = CASES["periodic"]
     for every in (1, c["nsteps"]):
         r2, g2 = loss_and_grad(s, c, st, every=every)
-        assert r2["loss"] == pytest.approx(r["loss"], rel=1e-14)
+        assert r2["loss"] == r["loss"]  # fixed-order reductions
         for n in "uvwp":
             np.testing.assert_array_equal(g2[n], g[n])
-        assert r2["dloss_dalpha"] == pytest.approx(r["dloss_dalpha"], rel=1e-12)
+        assert r2["dloss_dalpha"] == r["dloss_dalpha"]
 
 
 def test_backward_with_seeds_matches_ke(fp64_runs):
