@@ -8,6 +8,7 @@
 // replays every step of a run without re-capture.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <memory>
@@ -206,8 +207,11 @@ struct Impl final : ImplBase {
     if (cap_stream) cudaStreamDestroy(cap_stream);
   }
 
+  bool fuse_divergence = true;
+
   int init(mifgpu_ctx *ctx) override {
     g = ctx->g;
+    if (const char *fd = std::getenv("MIFGPU_FUSED_DIVERGENCE")) fuse_divergence = std::atoi(fd) != 0;
     field_elems = (size_t)g.PX * g.PY * g.PZ;
     cudaError_t e = cudaMalloc(&block, sizeof(T) * field_elems * kNumFields);
     if (e != cudaSuccess) return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the field block failed");
@@ -310,7 +314,7 @@ struct Impl final : ImplBase {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
     // The divergence is fused into the x-forward sweep unless the boundary
     // flux of the non-homogeneous Neumann problem has to be added in between.
-    const bool fused = solve && !nhn;
+    const bool fused = solve && !nhn && fuse_divergence;
     if (!fused) {
       mark(MIFGPU_PROF_DIVERGENCE, s);
       launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);

@@ -282,17 +282,31 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
   const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
   const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
   constexpr int nf = kUseP ? 4 : 3;
+  // The tile elements this thread copies (at most two of the kPL) and their
+  // in-plane offsets, computed once.
+  constexpr int kPer = (kPL + kTX * kTY - 1) / (kTX * kTY);
+  long off[kPer];
+  bool okk[kPer];
+#pragma unroll
+  for (int r = 0; r < kPer; ++r) {
+    const int e = threadIdx.x + r * kTX * kTY;
+    const int hx = e % kHX, hy = e / kHX;
+    const int i = i0 - 1 + hx, j = j0 - 1 + hy;
+    okk[r] = e < kPL && i < g.PX && j < g.PY;
+    off[r] = (long)i + g.PX * (long)j;
+  }
+  const long plane = g.sz();
   auto load_plane = [&](int kk) {
     if (kk >= 0 && kk < g.PZ) {
-      for (int e = threadIdx.x; e < kPL; e += kTX * kTY) {
-        const int hx = e % kHX, hy = e / kHX;
-        const int i = i0 - 1 + hx, j = j0 - 1 + hy;
-        const bool ok = i < g.PX && j < g.PY;
-        const long q = g.idx(i, j, kk);
+#pragma unroll
+      for (int r = 0; r < kPer; ++r) {
+        const int e = threadIdx.x + r * kTX * kTY;
+        if (e >= kPL) break;
+        const long q = off[r] + kk * plane;
 #pragma unroll
         for (int f = 0; f < nf; ++f) {
           T *d = &ring.f[f][kk & 3][e];
-          if (ok)
+          if (okk[r])
             cp_async_elem(d, src[f] + q);
           else
             *d = T(0);
@@ -451,17 +465,39 @@ __global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int d, int scal
 
 // ---- Poisson right-hand side and projection ----
 
+// Each thread owns kDivKZ consecutive owner planes of one (i, j) column; the
+// loads of all its points are issued before any result is stored.
+constexpr int kDivKZ = 4;
+
 template <typename T>
-__global__ void divergence_kernel(Geometry g, T *phi, const T *u, const T *v, const T *w, T inv_dt) {
+__global__ void __launch_bounds__(128) divergence_kernel(Geometry g, T *__restrict__ phi, const T *__restrict__ u,
+                                                         const T *__restrict__ v, const T *__restrict__ w, T inv_dt) {
   const int i = g.own_lo[0] + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = g.own_lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = g.own_lo[2] + blockIdx.z;
+  const int kb = g.own_lo[2] + blockIdx.z * kDivKZ;
+  const int ke = min(kb + kDivKZ, g.own_lo[2] + g.np[2]);
   if (i >= g.own_lo[0] + g.np[0] || j >= g.own_lo[1] + g.np[1]) return;
-  const long q = g.idx(i, j, k);
-  const T du = (ld(u, q + 1) - ld(u, q)) * T(g.oh[0]);
-  const T dv = (ld(v, q + g.sy()) - ld(v, q)) * T(g.oh[1]);
-  const T dw = (ld(w, q + g.sz()) - ld(w, q)) * T(g.oh[2]);
-  phi[q] = (du + dv + dw) * inv_dt;
+  const long q0 = g.idx(i, j, kb), sy = g.sy(), sz = g.sz();
+  T a[kDivKZ], b[kDivKZ], c[kDivKZ], d[kDivKZ], e[kDivKZ + 1];
+  e[0] = ld(w, q0);
+#pragma unroll
+  for (int r = 0; r < kDivKZ; ++r) {
+    if (kb + r >= ke) break;
+    const long q = q0 + r * sz;
+    a[r] = ld(u, q + 1);
+    b[r] = ld(u, q);
+    c[r] = ld(v, q + sy);
+    d[r] = ld(v, q);
+    e[r + 1] = ld(w, q + sz);
+  }
+#pragma unroll
+  for (int r = 0; r < kDivKZ; ++r) {
+    if (kb + r >= ke) break;
+    const T du = (a[r] - b[r]) * T(g.oh[0]);
+    const T dv = (c[r] - d[r]) * T(g.oh[1]);
+    const T dw = (e[r + 1] - e[r]) * T(g.oh[2]);
+    phi[q0 + r * sz] = (du + dv + dw) * inv_dt;
+  }
 }
 
 template <typename T>
@@ -491,21 +527,50 @@ __global__ void neumann_flux_serial_kernel(Geometry g, T *phi, int kind, TimeRef
   phi[q] = r;
 }
 
+// Each thread owns kProjKZ consecutive planes of one (i, j) column.
+constexpr int kProjKZ = 4;
+
 template <typename T>
-__global__ void project_kernel(Geometry g, T *p, const T *phi, T *u, T *v, T *w, T dt) {
+__global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict__ p, const T *__restrict__ phi,
+                                                      T *__restrict__ u, T *__restrict__ v, T *__restrict__ w, T dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  const long q = g.idx(i, j, k);
-  if (i < g.E[0] && j < g.E[1] && k < g.E[2]) p[q] = p[q] + ld(phi, q);
+  const int kb = blockIdx.z * kProjKZ;
+  const long sy = g.sy(), sz = g.sz();
   T *vel[3] = {u, v, w};
-  const long sc[3] = {1, g.sy(), g.sz()};
+  const long sc[3] = {1, sy, sz};
+  T ph[kProjKZ + 1], nb[2][kProjKZ], pv[kProjKZ], vv[3][kProjKZ];
+  // loads: phi at the points, their -x and -y neighbours, the plane below, p and the velocity
+  ph[0] = (kb >= 1 && i < g.E[0] && j < g.E[1] && kb - 1 < g.E[2]) ? ld(phi, g.idx(i, j, kb - 1)) : T(0);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
-    const T gp = (ld(phi, q) - ld(phi, q - sc[c])) * T(g.oh[c]);
-    vel[c][q] = vel[c][q] - gp * dt;
+  for (int r = 0; r < kProjKZ; ++r) {
+    const int k = kb + r;
+    const long q = g.idx(i, j, k);
+    const bool inp = i < g.E[0] && j < g.E[1] && k < g.E[2];
+    ph[r + 1] = inp ? ld(phi, q) : T(0);
+    nb[0][r] = (inp && i >= 1) ? ld(phi, q - 1) : T(0);
+    nb[1][r] = (inp && j >= 1) ? ld(phi, q - sy) : T(0);
+    pv[r] = inp ? p[q] : T(0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const bool in = i >= 1 && j >= 1 && k >= 1 && i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
+      vv[c][r] = in ? vel[c][q] : T(0);
+    }
   }
+#pragma unroll
+  for (int r = 0; r < kProjKZ; ++r) {
+    const int k = kb + r;
+    const long q = g.idx(i, j, k);
+    if (i < g.E[0] && j < g.E[1] && k < g.E[2]) p[q] = pv[r] + ph[r + 1];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
+      const T below = c == 0 ? nb[0][r] : (c == 1 ? nb[1][r] : ph[r]);
+      const T gp = (ph[r + 1] - below) * T(g.oh[c]);
+      vel[c][q] = vv[c][r] - gp * dt;
+    }
+  }
+  (void)sc;
 }
 
 // ---- layout conversion and initial fields ----
@@ -786,7 +851,7 @@ void launch_periodic_scalar(const Geometry &g, T *f, cudaStream_t s, long long *
 template <typename T>
 void launch_divergence(const Geometry &g, T *phi, T *const vel[3], double dt, cudaStream_t s, long long *launches) {
   const dim3 blk(32, 4, 1);
-  const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), (unsigned)g.np[2]);
+  const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZ));
   divergence_kernel<T><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt));
   if (launches) ++*launches;
 }
@@ -804,7 +869,7 @@ void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], doub
                     long long *launches) {
   const dim3 blk(32, 4, 1);
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
-  const dim3 grid(cdiv(ni, 32), cdiv(g.Es[1], 4), (unsigned)g.Es[2]);
+  const dim3 grid(cdiv(ni, 32), cdiv(g.Es[1], 4), cdiv(g.Es[2], kProjKZ));
   project_kernel<T><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt));
   if (launches) ++*launches;
 }
