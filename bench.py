@@ -56,13 +56,18 @@ WORKLOADS = {
 
 # Algorithmic HBM sweeps (full-field reads + writes) per launch of each kernel
 # class; times the field bytes and the cell count give algorithmic bytes.
-SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 4.0, "y_forward": 2.0, "z_fused": 2.0,
+SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 2.0, "y_forward": 2.0, "z_fused": 2.0,
           "y_inverse": 2.0, "x_inverse": 2.0, "project": 9.0}
 LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3, "z_fused": 3, "y_inverse": 3,
                      "x_inverse": 3, "project": 3}
-MEASURED_TRAFFIC_RATIO = {"stage": 1.01, "x_forward": 1.01, "y_forward": 0.83, "z_fused": 0.91, "y_inverse": 0.83,
-                          "x_inverse": 0.82}
-STEP_SWEEPS = 90.0  # per step: 33 stage + 3 x (4 + 5 x 2 + 9) Poisson/projection, minus fusions not done
+# DRAM read + write bytes over algorithmic bytes, from one ncu capture of the
+# 256x256x512 profiling case (profiles/): applied to the full launch.
+MEASURED_TRAFFIC_RATIO = {"stage": 1.05, "y_forward": 0.83, "z_fused": 0.91, "y_inverse": 0.83, "x_inverse": 0.82}
+# Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps + 9 projection).
+STEP_SWEEPS = 102.0
+# The same step with the divergence fused into the x-forward sweep and the
+# projection into the x-inverse sweep (the fused dataflow): 90 sweeps.
+FUSED_STEP_SWEEPS = 90.0
 
 
 def measured_peaks():
@@ -499,7 +504,10 @@ def run_gpu(args):
                        (11 * elem * cells / 1e9)},
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "step_roofline": {"bytes_per_cell_step": STEP_SWEEPS * elem, "achieved_gbs": round(step_roofline, 1),
-                              "frac": round(step_roofline / peak, 4)},
+                              "frac": round(step_roofline / peak, 4),
+                              "fused_dataflow_bytes_per_cell_step": FUSED_STEP_SWEEPS * elem,
+                              "fused_dataflow_frac": round(step_roofline * FUSED_STEP_SWEEPS / STEP_SWEEPS / peak,
+                                                           4)},
             "kernel_ms_per_step": {k: round(v, 4) for k, v in prof.items()},
             "error": linf, "fp64": fp64, "adjoint": adjoint, "cpu_baseline": cpu,
         }

@@ -8,7 +8,6 @@
 // replays every step of a run without re-capture.
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <memory>
@@ -207,11 +206,8 @@ struct Impl final : ImplBase {
     if (cap_stream) cudaStreamDestroy(cap_stream);
   }
 
-  bool fuse_divergence = true;
-
   int init(mifgpu_ctx *ctx) override {
     g = ctx->g;
-    if (const char *fd = std::getenv("MIFGPU_FUSED_DIVERGENCE")) fuse_divergence = std::atoi(fd) != 0;
     field_elems = (size_t)g.PX * g.PY * g.PZ;
     cudaError_t e = cudaMalloc(&block, sizeof(T) * field_elems * kNumFields);
     if (e != cudaSuccess) return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the field block failed");
@@ -312,18 +308,16 @@ struct Impl final : ImplBase {
   void enqueue_pressure(mifgpu_ctx *ctx, cudaStream_t s, int set, double dt, bool nhn, int slot_new, int slot_old,
                         bool solve, long long *cnt) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
-    // The divergence is fused into the x-forward sweep unless the boundary
-    // flux of the non-homogeneous Neumann problem has to be added in between.
-    const bool fused = solve && !nhn && fuse_divergence;
-    if (!fused) {
-      mark(MIFGPU_PROF_DIVERGENCE, s);
-      launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
-      if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
-    }
+    // The divergence is its own streaming kernel: fused into the x-forward
+    // sweep (PoissonSolver::solve's `vel` argument) its loads ran at the line
+    // kernel's low occupancy and the pair took 2.5x longer on GB300.
+    mark(MIFGPU_PROF_DIVERGENCE, s);
+    launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
+    if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
     if (!solve) return;
     std::function<void(int)> mk;
     if (prof) mk = [&](int q) { mark(MIFGPU_PROF_X_FORWARD + q, s); };
-    ps.solve(F.f[kPhi], s, cnt, mk, fused ? vel : nullptr, dt);
+    ps.solve(F.f[kPhi], s, cnt, mk);
     mark(MIFGPU_PROF_PERIODIC, s);
     launch_periodic_scalar<T>(g, F.f[kPhi], s, cnt);
   }

@@ -282,31 +282,17 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
   const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
   const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
   constexpr int nf = kUseP ? 4 : 3;
-  // The tile elements this thread copies (at most two of the kPL) and their
-  // in-plane offsets, computed once.
-  constexpr int kPer = (kPL + kTX * kTY - 1) / (kTX * kTY);
-  long off[kPer];
-  bool okk[kPer];
-#pragma unroll
-  for (int r = 0; r < kPer; ++r) {
-    const int e = threadIdx.x + r * kTX * kTY;
-    const int hx = e % kHX, hy = e / kHX;
-    const int i = i0 - 1 + hx, j = j0 - 1 + hy;
-    okk[r] = e < kPL && i < g.PX && j < g.PY;
-    off[r] = (long)i + g.PX * (long)j;
-  }
-  const long plane = g.sz();
   auto load_plane = [&](int kk) {
     if (kk >= 0 && kk < g.PZ) {
-#pragma unroll
-      for (int r = 0; r < kPer; ++r) {
-        const int e = threadIdx.x + r * kTX * kTY;
-        if (e >= kPL) break;
-        const long q = off[r] + kk * plane;
+      for (int e = threadIdx.x; e < kPL; e += kTX * kTY) {
+        const int hx = e % kHX, hy = e / kHX;
+        const int i = i0 - 1 + hx, j = j0 - 1 + hy;
+        const bool ok = i < g.PX && j < g.PY;
+        const long q = g.idx(i, j, kk);
 #pragma unroll
         for (int f = 0; f < nf; ++f) {
           T *d = &ring.f[f][kk & 3][e];
-          if (okk[r])
+          if (ok)
             cp_async_elem(d, src[f] + q);
           else
             *d = T(0);
