@@ -1,11 +1,20 @@
 """Throughput of one GB300 projection step (Gcell-steps/s), JSON on one line.
 
-Workload (default): the manufactured-solution unit cube at 512^3 cells
-(513^3 nodes, every face Dirichlet, homogeneous-Neumann DCT-I Poisson),
-Re = 1000, dt = 1e-4 (64/512)^2 (dt scaled with h^2 as in the large
-manufactured runs), SINCOS velocity with its Navier-Stokes forcing, mixed
-precision (f32 storage and stencils, f64 eigenvalue division). Inputs are the
-analytic fields at t = 0, generated on the device (synthetic; no dataset).
+Workload (default): the reference's own full-step test case (test/full_test.cpp),
+the Ethier-Steinman exact Navier-Stokes solution, on the unit cube at 512^3
+cells (513^3 nodes, every face Dirichlet with the exact velocity,
+homogeneous-Neumann DCT-I Poisson), Re = 1000, dt = 1e-4 (64/512)^2 (dt
+scaled with h^2 as in the large manufactured runs), no forcing (mif::timestep
+unchanged), mixed precision (f32 storage and stencils, f64 eigenvalue
+division). Inputs are the analytic fields at t = 0, generated on the device
+(synthetic; no dataset). The L-infinity velocity error against the exact
+solution after the run is reported for the mixed run and for the FP64 run of
+the same workload (the matched-error comparison).
+
+Extra modes (each prints one JSON line): --configs runs the reference's
+benchmark configurations 1-3 at their sizes; --sweep runs the Ethier-Steinman
+refinement 32^3 -> 768^3 in FP64 and mixed precision (convergence order and
+matched error); --adjoint-only runs the adjoint workload alone.
 
 Arms:
   --impl gb300      (default) the CUDA library: `value` from CUDA events around
@@ -44,8 +53,15 @@ UNIT = "Gcell-steps/s"
 
 WORKLOADS = {
     # name: (n_global, size, origin, periodic, Re, dt, kind, forcing)
+    # The reference's own full-step case (test/full_test.cpp): the Ethier-Steinman
+    # exact Navier-Stokes solution on the unit cube, no forcing (mif::timestep as is).
     "cube512": ((513, 513, 513), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
-                1e-4 * (64.0 / 512.0) ** 2, 1, 2),
+                1e-4 * (64.0 / 512.0) ** 2, 2, 0),
+    "cube768": ((769, 769, 769), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
+                1e-4 * (64.0 / 768.0) ** 2, 2, 0),
+    # SINCOS velocity with its Navier-Stokes forcing (the forcing extension)
+    "cube512_sincos": ((513, 513, 513), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
+                       1e-4 * (64.0 / 512.0) ** 2, 1, 2),
     "channel512x256x512": ((513, 257, 513), (4 * 3.141592653589793, 2.0, 2 * 3.141592653589793), (0.0, 0.0, 0.0),
                            (True, False, True), 5000.0, 5e-4, 0, 0),
     "cube64": ((65, 65, 65), (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0, 1e-4, 1, 2),
@@ -175,10 +191,10 @@ def replica_throughput(ms_local: float, world: int, cells: int, steps: int) -> t
 # ---------------------------------------------------------------- CPU baseline
 
 def _cpu_worker(args):
-    n, steps, periodic, size, Re, dt, kind = args
+    n, steps, periodic, size, Re, dt, kind, forcing = args
     import oracle as O
 
-    case = O.Case(n_global=(n, n, n), size=size, Re=Re, dt=dt, periodic=periodic, exact_kind=kind, forcing=2)
+    case = O.Case(n_global=(n, n, n), size=size, Re=Re, dt=dt, periodic=periodic, exact_kind=kind, forcing=forcing)
     s = O.OracleSolver(case)
     s.set_exact_velocity(0, 0.0, True)
     s.set_exact_pressure(0.0)
@@ -200,7 +216,7 @@ def cpu_baseline(workers: int, n: int = 97, steps: int = 3):
 
     O.build(with_ref=False)
     w = WORKLOADS["cube512"]
-    job = (n, steps, w[3], w[1], w[4], w[5], w[6])
+    job = (n, steps, w[3], w[1], w[4], w[5], w[6], w[7])
     t0 = time.perf_counter()
     if workers == 1:
         res = [_cpu_worker(job)]
@@ -212,7 +228,8 @@ def cpu_baseline(workers: int, n: int = 97, steps: int = 3):
     cells = sum(r[0] for r in res)
     per_worker = max(r[1] for r in res)
     return {"value": cells / per_worker / 1e9, "unit": UNIT, "cores": workers, "kind": "port",
-            "sample": f"{n - 1}^3-cell manufactured cube (SINCOS + NS forcing), {steps} steps per core after "
+            "sample": f"{n - 1}^3-cell Ethier-Steinman cube (the default workload at a smaller size), {steps} steps "
+                      f"per core after "
                       f"1 warm-up, {workers} independent replicas, oracle/mif_oracle.c built -O2 "
                       f"(wall {wall:.1f}s)"}
 
@@ -355,6 +372,217 @@ def adjoint_bench(stream):
         float(np.abs(g32[nm] - g64[nm]).max() / np.abs(g64[nm]).max()) for nm in "uvw")
     res["fp32_vs_fp64_dalpha_rel_err"] = abs(r32["dloss_dalpha"] - r64["dloss_dalpha"]) / abs(r64["dloss_dalpha"])
     return res
+
+
+# ------------------------------------------------------------------ reference configurations
+
+def solenoidal_noise(shape_of, ncell, L, base, kmax, amp, seed):
+    """Seeded divergence-free noise on a staggered grid: the curl of a Gaussian
+    vector potential with |A_k| ~ |k|^-2 (integer wavenumbers, 0 < |k| <= kmax),
+    periodic over the box, scaled to max |u| = amp. Component c is sampled at
+    its own staggered points by a spectral phase shift; array index i along
+    axis d maps to grid point (base_d + i) mod ncell_d."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = ncell
+    kx = np.fft.rfftfreq(nx, 1.0 / nx)
+    ky = np.fft.fftfreq(ny, 1.0 / ny)
+    kz = np.fft.fftfreq(nz, 1.0 / nz)
+    KZ, KY, KX = np.meshgrid(kz, ky, kx, indexing="ij")
+    kk = np.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
+    mask = (kk > 0) & (kk <= kmax)
+    A = []
+    for _ in range(3):
+        a = np.zeros(kk.shape, np.complex64)
+        m = int(mask.sum())
+        a[mask] = (rng.standard_normal(m) + 1j * rng.standard_normal(m)) / kk[mask] ** 2
+        A.append(a)
+    w = [2 * np.pi / L[d] for d in range(3)]
+    K = (KX * w[0], KY * w[1], KZ * w[2])
+    uh = (1j * (K[1] * A[2] - K[2] * A[1]), 1j * (K[2] * A[0] - K[0] * A[2]), 1j * (K[0] * A[1] - K[1] * A[0]))
+    vals = []
+    for c in range(3):
+        h = L[c] / ncell[c]
+        vals.append(np.fft.irfftn(uh[c] * np.exp(-1j * K[c] * h / 2), s=(nz, ny, nx)).astype(np.float64))
+    scale = amp / max(float(np.abs(f).max()) for f in vals)
+    out = {}
+    for c, name in enumerate("uvw"):
+        ez, ey, ex = shape_of(name)
+        ii = (base[0] + np.arange(ex)) % nx
+        jj = (base[1] + np.arange(ey)) % ny
+        kq = (base[2] + np.arange(ez)) % nz
+        out[name] = np.ascontiguousarray(vals[c][np.ix_(kq, jj, ii)] * scale)
+    return out
+
+
+def staggered_coords(s, name, n_global, size, origin, periodic):
+    """Positions (x, y, z) of a field's points, reference layout (z, y, x)."""
+    import numpy as np
+
+    ez, ey, ex = s.shape(name)
+    comp = "uvw".index(name) if name in "uvw" else -1
+    ax = []
+    for d, e in enumerate((ex, ey, ez)):
+        h = size[d] / (n_global[d] - 1)
+        base = -1 if periodic[d] else 0
+        x = origin[d] + h * (base + np.arange(e))
+        if d == comp:
+            x = x - h / 2
+        ax.append(x)
+    z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return x, y, z
+
+
+def timed_run(s, stream, t0, nsteps):
+    import torch
+
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.run(t0, nsteps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / nsteps
+
+
+def config_suite(stream):
+    """The reference's benchmark configurations 1-3 at their sizes, FP64 and
+    mixed: Gcell-steps/s, errors against the analytic solution (config 1) or
+    between the two precisions after the run (configs 2 and 3)."""
+    import numpy as np
+    import torch
+
+    import mifgpu
+
+    pi = 3.141592653589793
+    out = {}
+
+    def make(n_global, size, origin, periodic, Re, dt, prec, kind, forcing):
+        s = mifgpu.Solver(n_global=n_global, size=size, origin=origin, Re=Re, dt=dt, periodic=periodic,
+                          precision=prec, boundary_kind=kind, forcing=forcing)
+        s.set_stream(stream.cuda_stream)
+        return s
+
+    # 1: 64^3 manufactured cube, SINCOS + forcing, FP64, 10 steps of 1e-4
+    c1 = {}
+    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+        s = make((65,) * 3, (1.0,) * 3, (0.0,) * 3, (False,) * 3, 1000.0, 1e-4, prec, 1, 2)
+        s.set_exact_velocity(0, 0.0)
+        s.set_exact_pressure(0.0)
+        s.run(0.0, 2)
+        s.set_exact_velocity(0, 0.0)
+        s.set_exact_pressure(0.0)
+        ms = timed_run(s, stream, 0.0, 10)
+        s.adjust_pressure(10 * 1e-4)
+        nrm = s.error_norms(10 * 1e-4)
+        c1[pname] = {"ms_per_step": round(ms, 4), "gcell_steps_s": 64 ** 3 / ms / 1e6,
+                     "velocity_l2": nrm[1], "velocity_linf": nrm[2], "pressure_l2": nrm[4], "pressure_linf": nrm[5]}
+        s.close()
+    out["1_cube64_manufactured"] = c1
+
+    # 2: periodic 256^3 Taylor-Green + k^-2 noise (|k| <= 16, 1e-2), Re 1600, dt 2e-3, 100 steps
+    n_g = (257,) * 3
+    size = (2 * pi,) * 3
+    fields = {}
+    c2 = {}
+    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+        s = make(n_g, size, (0.0,) * 3, (True,) * 3, 1600.0, 2e-3, prec, 0, 0)
+        if not fields:
+            noise = solenoidal_noise(s.shape, (256,) * 3, size, (-1,) * 3, 16, 1e-2, 11)
+            for c, nm in enumerate("uvw"):
+                x, y, z = staggered_coords(s, nm, n_g, size, (0.0,) * 3, (True,) * 3)
+                base = (np.sin(x) * np.cos(y) * np.cos(z) if c == 0 else
+                        -np.cos(x) * np.sin(y) * np.cos(z) if c == 1 else 0.0 * x)
+                fields[nm] = base + noise[nm]
+            fields["p"] = np.zeros(s.shape("p"))
+        s.load_state(fields)
+        s.run(0.0, 2)
+        s.load_state(fields)
+        ms = timed_run(s, stream, 0.0, 100)
+        c2[pname] = {"ms_per_step": round(ms, 4), "gcell_steps_s": 256 ** 3 / ms / 1e6,
+                     "final": {nm: s.download(nm) for nm in "uvw"}}
+        s.close()
+        torch.cuda.empty_cache()
+    umax = max(float(np.abs(c2["fp64"]["final"][nm]).max()) for nm in "uvw")
+    c2["mixed_vs_fp64_velocity_linf"] = max(
+        float(np.abs(c2["mixed"]["final"][nm] - c2["fp64"]["final"][nm]).max()) for nm in "uvw") / umax
+    for pname in ("fp64", "mixed"):
+        del c2[pname]["final"]
+    c2["mixed_speedup"] = round(c2["fp64"]["ms_per_step"] / c2["mixed"]["ms_per_step"], 2)
+    out["2_tgv256_periodic"] = c2
+
+    # 3: channel [0,4pi]x[0,2]x[0,2pi], 512x256x512, periodic x z, walls in y, Re 5000, dt 5e-4, 50 steps
+    n_g = (513, 257, 513)
+    size = (4 * pi, 2.0, 2 * pi)
+    per = (True, False, True)
+    fields = {}
+    c3 = {}
+    for pname, prec in (("mixed", mifgpu.MIXED), ("fp64", mifgpu.FP64)):
+        s = make(n_g, size, (0.0,) * 3, per, 5000.0, 5e-4, prec, 0, 0)
+        if not fields:
+            noise = solenoidal_noise(s.shape, (512, 256, 512), size, (-1, 0, -1), 16, 1e-2, 12)
+            for nm in "uvw":
+                x, y, z = staggered_coords(s, nm, n_g, size, (0.0,) * 3, per)
+                fields[nm] = (1.0 - (y - 1.0) ** 2 if nm == "u" else 0.0 * y) + noise[nm]
+                del x, z
+            fields["p"] = np.zeros(s.shape("p"))
+        s.load_state(fields)
+        s.run(0.0, 2)
+        s.load_state(fields)
+        ms = timed_run(s, stream, 0.0, 50)
+        c3[pname] = {"ms_per_step": round(ms, 4), "gcell_steps_s": 512 * 256 * 512 / ms / 1e6,
+                     "final": {nm: s.download(nm) for nm in "uvw"}}
+        s.close()
+        torch.cuda.empty_cache()
+    umax = max(float(np.abs(c3["fp64"]["final"][nm]).max()) for nm in "uvw")
+    c3["mixed_vs_fp64_velocity_linf"] = max(
+        float(np.abs(c3["mixed"]["final"][nm] - c3["fp64"]["final"][nm]).max()) for nm in "uvw") / umax
+    for pname in ("fp64", "mixed"):
+        del c3[pname]["final"]
+    c3["mixed_speedup"] = round(c3["fp64"]["ms_per_step"] / c3["mixed"]["ms_per_step"], 2)
+    out["3_channel512x256x512"] = c3
+    return out
+
+
+def sweep(stream, sizes=(32, 64, 128, 256, 512, 768)):
+    """Ethier-Steinman refinement (the reference's full-step test case on the
+    unit cube): 2 steps of dt = 5e-5 from t = 0, FP64 and mixed, L-infinity
+    velocity and pressure errors against the exact solution, observed orders."""
+    import torch
+
+    import mifgpu
+
+    T, nt = 1e-4, 2
+    rows = []
+    for n in sizes:
+        row = {"cells": n}
+        for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+            s = mifgpu.Solver(n_global=(n + 1,) * 3, Re=1000.0, dt=T / nt, precision=prec,
+                              boundary_kind=mifgpu.FIELD_ETHIER)
+            s.set_stream(stream.cuda_stream)
+            s.set_exact_velocity(0, 0.0)
+            s.set_exact_pressure(0.0)
+            s.run(0.0, 1)
+            s.set_exact_velocity(0, 0.0)
+            s.set_exact_pressure(0.0)
+            ms = timed_run(s, stream, 0.0, nt)
+            s.adjust_pressure(T)
+            nrm = s.error_norms(T)
+            row[pname] = {"velocity_linf": nrm[2], "pressure_linf": nrm[5], "ms_per_step": round(ms, 4)}
+            s.close()
+            torch.cuda.empty_cache()
+        row["mixed_over_fp64_velocity_linf"] = row["mixed"]["velocity_linf"] / row["fp64"]["velocity_linf"]
+        rows.append(row)
+    import math
+
+    for a, b in zip(rows, rows[1:]):
+        for pname in ("fp64", "mixed"):
+            b[pname]["velocity_order"] = math.log(a[pname]["velocity_linf"] / b[pname]["velocity_linf"]) / \
+                math.log(b["cells"] / a["cells"])
+            b[pname]["pressure_order"] = math.log(a[pname]["pressure_linf"] / b[pname]["pressure_linf"]) / \
+                math.log(b["cells"] / a["cells"])
+    return {"case": "Ethier-Steinman on [0,1]^3, Re=1000, T=1e-4 in 2 steps (test/full_test.cpp)", "rows": rows}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -533,7 +761,7 @@ def run_reference(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "n_global": list(n_global), "sample": "64^3 cells per core"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"64^3-cell manufactured cube, 1 step per core per bench step, {cores} "
+                             "sample": f"64^3-cell Ethier-Steinman cube, 1 step per core per bench step, {cores} "
                                        f"independent replicas (wall {el:.1f}s)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -551,6 +779,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--configs", action="store_true", help="the reference's configurations 1-3 (one JSON line)")
+    ap.add_argument("--sweep", action="store_true", help="Ethier-Steinman refinement 32^3..768^3 (one JSON line)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="only the adjoint workload (a profiling aid; prints {'adjoint': ...})")
     args = ap.parse_args()
@@ -558,6 +788,14 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.configs or args.sweep:
+        import torch
+
+        import build as pkg_build
+
+        pkg_build.build()
+        stream = torch.cuda.Stream()
+        print(json.dumps({"configs": config_suite(stream)} if args.configs else {"sweep": sweep(stream)}))
     elif args.adjoint_only:
         import torch
 

@@ -17,9 +17,15 @@ struct AxisPlan {
   int nfac = 0;
   int fac[16] = {0};
   int P = 1, lg_lines = 1;
-  // register-resident path (float, power-of-two L): L = reg_n1 * reg_n2, 0 if unused
-  int reg_n1 = 0, reg_n2 = 0, reg_P = 0, reg_lg = 0;
+  // register-resident path (float): FFT length reg_L = reg_n1 * reg_n2 (a power
+  // of two in 64..1024), 0 if unused. A DCT-I axis of n = N + 1 points runs as
+  // one length-N transform per line pair (reg_half, kernel kind 2); a periodic
+  // axis as its length-n real DFT.
+  int reg_n1 = 0, reg_n2 = 0, reg_P = 0, reg_lg = 0, reg_L = 0;
+  bool reg_half = false;
   size_t reg_smem = 0;
+  typename Vec2<T>::type *reg_tw = nullptr;  // exp(-2 pi i e / reg_L)
+  typename Vec2<T>::type *dsc = nullptr;     // (sin, cos)(pi j / N), j < N (reg_half)
   bool pow2 = false;
   bool line_fast = false;
   size_t smem = 0;

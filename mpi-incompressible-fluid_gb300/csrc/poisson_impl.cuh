@@ -59,10 +59,12 @@ struct LineArgs {
   T *data;
   long se, sa, sb, base;  // element stride, strides of the two other axes, owner-block origin
   int na, nb;             // owner points along the two other axes (a varies fastest)
-  int n, L, kind;         // points per line, complex FFT length, 0 DCT-I / 1 real DFT
+  int n, L, kind;         // points per line, complex FFT length, 0 DCT-I / 1 real DFT /
+                          // 2 DCT-I as a length n-1 transform (register path)
   FftFactors fac;
   int pow2;               // L is a power of two (shift-indexed FFT stages)
   const typename Vec2<T>::type *tw;
+  const typename Vec2<T>::type *dsc;  // register path, kind 2: (sin, cos)(pi j / N)
   int P, lg_lines;        // line pairs per CTA; log2(2P)
   int line_fast;          // 1: consecutive threads take consecutive lines (strided axes)
   double scale;           // output multiplier (inverse normalisation), 1 otherwise
@@ -338,6 +340,92 @@ __device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, 
   }
 }
 
+// DCT-I of N + 1 points (FFTW's REDFT00, unnormalised) from one length-N
+// transform (the classic half-length algorithm): with s_j = x_j + x_{N-j} and
+// d_j = x_j - x_{N-j}, the DFT Y of y_j = s_j / 2 - sin(pi j / N) d_j gives
+//   X_{2k} = 2 Re Y_k,  X_{2k+1} = X_{2k-1} - 2 Im Y_k,
+//   X_1 = sum_j d_j cos(pi j / N).
+// Two lines travel as z = a + i b; their Y_k are split from Z_k and Z_{N-k}.
+
+// Input element m < N of z for the pair, and the pair's partial X_1.
+template <typename T>
+__device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row, int m, int N,
+                                               const typename Vec2<T>::type *dsc, typename Vec2<T>::type &v,
+                                               typename Vec2<T>::type &x1) {
+  using T2 = typename Vec2<T>::type;
+  const T2 xm = row[m], xn = row[N - m];
+  const T2 sc = __ldg(dsc + m);
+  const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
+  v.x = T(0.5) * sx - sc.x * dx;
+  v.y = T(0.5) * sy - sc.x * dy;
+  x1.x += sc.y * dx;
+  x1.y += sc.y * dy;
+}
+
+// row[k] = Z_k (k < N) of the pair -> row[m] = X_m (m <= N) of both lines.
+// Thread t of the pair's N2 handles k in [t C, t C + C), C = N / (2 N2): the
+// even outputs directly, the odd ones as a running sum within the thread plus
+// an exclusive scan of the thread totals across the pair's lanes (the pair's
+// N2 threads are consecutive lanes of one warp).
+template <typename T, int N1, int N2>
+__device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int t, typename Vec2<T>::type x1) {
+  using T2 = typename Vec2<T>::type;
+  constexpr int N = N1 * N2, C = N1 / 2;
+  static_assert(N2 <= 32 && (N1 % 2) == 0, "pair within one warp");
+#pragma unroll
+  for (int o = N2 / 2; o > 0; o >>= 1) {
+    x1.x += __shfl_xor_sync(0xffffffffu, x1.x, o, N2);
+    x1.y += __shfl_xor_sync(0xffffffffu, x1.y, o, N2);
+  }
+  T2 ev[C], od[C];
+  T2 run = {T(0), T(0)};
+  const int kb = t * C;
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int k = kb + c;
+    const T2 zk = row[k], zn = row[(N - k) & (N - 1)];
+    ev[c].x = zk.x + zn.x;
+    ev[c].y = zk.y + zn.y;
+    if (k > 0) {
+      run.x -= zk.y - zn.y;
+      run.y += zk.x - zn.x;
+    }
+    od[c] = run;
+  }
+  T2 incl = run;
+#pragma unroll
+  for (int o = 1; o < N2; o <<= 1) {
+    const T ux = __shfl_up_sync(0xffffffffu, incl.x, o, N2);
+    const T uy = __shfl_up_sync(0xffffffffu, incl.y, o, N2);
+    if (t >= o) {
+      incl.x += ux;
+      incl.y += uy;
+    }
+  }
+  T2 excl;
+  excl.x = __shfl_up_sync(0xffffffffu, incl.x, 1, N2);
+  excl.y = __shfl_up_sync(0xffffffffu, incl.y, 1, N2);
+  if (t == 0) excl.x = excl.y = T(0);
+  const T2 zh = row[N / 2];
+  __syncthreads();  // every thread has read its Z values
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int k = kb + c;
+    row[2 * k] = ev[c];
+    T2 o;
+    o.x = x1.x + (excl.x + od[c].x);
+    o.y = x1.y + (excl.y + od[c].y);
+    row[2 * k + 1] = o;
+  }
+  if (t == N2 - 1) {
+    T2 e;
+    e.x = T(2) * zh.x;
+    e.y = T(2) * zh.y;
+    row[N] = e;
+  }
+  __syncthreads();
+}
+
 // One length-L forward FFT (exponent sign -1) of the pair owned by this
 // thread group, in two register passes; x holds the thread's inputs
 // x[n1] = z[n1*N2 + t] and the result X[k] lands in row[k], conjugated when
@@ -459,19 +547,26 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
     // product and the inverse transform of the z sweep
     const bool plus = KIND == 1 && (MODE == kModeInverse || pass == 1);
     if (pass == 1) {
-      reg_eig_row<T, L, KIND>(row, t, N2, n, ea, eb);
+      reg_eig_row<T, L, KIND == 2 ? 0 : KIND>(row, t, N2, n, ea, eb);
       __syncthreads();
     }
     T2 x[N1];
+    T2 x1 = {T(0), T(0)};  // kind 2: the pair's partial X_1
 #pragma unroll
     for (int n1 = 0; n1 < N1; ++n1) {
       const int m = n1 * N2 + t;
-      T2 v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
-                       : row[KIND == 0 ? (m < n ? m : L - m) : m];
+      T2 v;
+      if (KIND == 2) {
+        dct_half_input<T>(row, m, L, a.dsc, v, x1);
+      } else {
+        v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
+                      : row[KIND == 0 ? (m < n ? m : L - m) : m];
+      }
       if (plus) v.y = -v.y;
       x[n1] = v;
     }
     reg_fft_core<T, N1, N2>(x, row, t, a.tw, plus);
+    if (KIND == 2) dct_half_output<T, N1, N2>(row, t, x1);
   }
   // store: row[m] holds X[m]; the forward real DFT splits the pair into
   // FFTW's half-complex order on the way out.
@@ -517,6 +612,10 @@ int smallest_radix(int L) {
 // (poisson_reg_*.cu), so the shapes compile in parallel.
 template <typename T, int A, int B>
 const void *reg_kernel_ptr(int mode, int kind) {
+  if (kind == 2)
+    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 2>
+           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 2>
+                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 2>;
   if (kind == 0)
     return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 0>
            : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 0>
@@ -603,13 +702,19 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
     for (int q = 0; q < nfac; ++q)
       if (fac[q] & (fac[q] - 1)) pow2 = false;
   smem = row_bytes * P;
-  // Register-resident path (regfft.cuh): float, power-of-two L in [64, 1024].
-  reg_n1 = reg_n2 = 0;
-  if (std::is_same<T, float>::value && (L & (L - 1)) == 0 && L >= 64 && L <= 1024) {
+  // Register-resident path (regfft.cuh): float, a power-of-two transform in
+  // [64, 1024]: the real DFT of a periodic line, or for a DCT-I line of
+  // n = N + 1 points the length-N transform of the half-length algorithm.
+  reg_n1 = reg_n2 = reg_L = 0;
+  reg_half = false;
+  const int cand = kind == 0 ? n - 1 : n;
+  if (std::is_same<T, float>::value && (cand & (cand - 1)) == 0 && cand >= 64 && cand <= 1024) {
+    reg_L = cand;
+    reg_half = kind == 0;
     int lg = 0;
-    while ((1 << lg) < L) ++lg;
+    while ((1 << lg) < reg_L) ++lg;
     reg_n1 = 1 << ((lg + 1) / 2);
-    reg_n2 = L / reg_n1;
+    reg_n2 = reg_L / reg_n1;
     reg_P = kThreads / reg_n2;
     reg_lg = 0;
     while ((1 << reg_lg) < 2 * reg_P) ++reg_lg;
@@ -629,6 +734,25 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
     return -2;
   }
   cudaMemcpy(tw, hw.data(), sizeof(hw[0]) * L, cudaMemcpyHostToDevice);
+  reg_tw = tw;
+  if (reg_n1 && reg_L != L) {
+    std::vector<typename Vec2<T>::type> rw(reg_L), sc(reg_L);
+    for (int e = 0; e < reg_L; ++e) {
+      const long double ang = two_pi * (long double)e / (long double)reg_L;
+      rw[e].x = (T)cosl(ang);
+      rw[e].y = (T)(-sinl(ang));
+      const long double half = ang / 2;  // pi e / N
+      sc[e].x = (T)sinl(half);
+      sc[e].y = (T)cosl(half);
+    }
+    if (cudaMalloc(&reg_tw, sizeof(rw[0]) * reg_L) != cudaSuccess ||
+        cudaMalloc(&dsc, sizeof(sc[0]) * reg_L) != cudaSuccess) {
+      err = "cudaMalloc of the half-length DCT tables failed";
+      return -2;
+    }
+    cudaMemcpy(reg_tw, rw.data(), sizeof(rw[0]) * reg_L, cudaMemcpyHostToDevice);
+    cudaMemcpy(dsc, sc.data(), sizeof(sc[0]) * reg_L, cudaMemcpyHostToDevice);
+  }
 
   // Eigenvalues of the discrete Laplacian along this axis, exactly as
   // src/PressureSolverStructures.cpp:5-11 computes them (double, host libm).
@@ -648,9 +772,11 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
 
 template <typename T>
 void AxisPlan<T>::release() {
+  if (reg_tw && reg_tw != tw) cudaFree(reg_tw);
+  if (dsc) cudaFree(dsc);
   if (tw) cudaFree(tw);
   if (lam_dev) cudaFree(lam_dev);
-  tw = nullptr;
+  tw = reg_tw = dsc = nullptr;
   lam_dev = nullptr;
 }
 
@@ -692,7 +818,7 @@ int PoissonSolver<T>::init(const Geometry &g, std::string &err) {
   for (int d = 0; d < 3; ++d) {
     if (!axis[d].reg_n1) continue;
     for (int mode = 0; mode < 3; ++mode) {
-      const void *fn = RegKernels<T>::get(axis[d].reg_n1, axis[d].reg_n2, mode, axis[d].kind);
+      const void *fn = RegKernels<T>::get(axis[d].reg_n1, axis[d].reg_n2, mode, axis[d].reg_half ? 2 : axis[d].kind);
       if (!fn || raise_dynamic_smem(fn, axis[d].reg_smem) != cudaSuccess) {
         err = "register-path kernel set-up failed";
         return -2;
@@ -771,6 +897,10 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
     if (ax.reg_n1) {
       a.P = ax.reg_P;
       a.lg_lines = ax.reg_lg;
+      a.L = ax.reg_L;
+      a.tw = ax.reg_tw;
+      a.dsc = ax.dsc;
+      if (ax.reg_half) a.kind = 2;
       const unsigned grid = (unsigned)((total + 2 * a.P - 1) / (2 * a.P));
       launch_reg<T>(ax.reg_n1, ax.reg_n2, mode, grid, ax.reg_smem, stream, a);
       if (launches) ++*launches;

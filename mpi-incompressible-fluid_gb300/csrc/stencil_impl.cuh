@@ -78,10 +78,19 @@ struct ForcingEval {
   T alpha;
   __device__ __forceinline__ T S(int ax, int face, int i) const { return tab[((ax * 2 + face) * 2 + 0) * maxE + i]; }
   __device__ __forceinline__ T C(int ax, int face, int i) const { return tab[((ax * 2 + face) * 2 + 1) * maxE + i]; }
-  __device__ __forceinline__ T operator()(int c, int i, int j, int k) const {
-    const T sx = S(0, c == 0, i), cx = C(0, c == 0, i);
-    const T sy = S(1, c == 1, j), cy = C(1, c == 1, j);
-    const T sz = S(2, c == 2, k), cz = C(2, c == 2, k);
+  // sin/cos at the node ([0]) and the face ([1]) coordinate of one index per axis.
+  struct Axis {
+    T s[2], c[2];
+  };
+  __device__ __forceinline__ Axis axis(int ax, int i) const {
+    return Axis{{S(ax, 0, i), S(ax, 1, i)}, {C(ax, 0, i), C(ax, 1, i)}};
+  }
+  // Component c at the staggered point with per-axis factors X, Y, Z (the
+  // x and y ones are constant through a thread's march in z).
+  __device__ __forceinline__ T eval(int c, const Axis &X, const Axis &Y, const Axis &Z) const {
+    const T sx = X.s[c == 0], cx = X.c[c == 0];
+    const T sy = Y.s[c == 1], cy = Y.c[c == 1];
+    const T sz = Z.s[c == 2], cz = Z.c[c == 2];
     T f;
     if (tg) return c == 0 ? alpha * (sx * cy * cz) : (c == 1 ? -alpha * (cx * sy * cz) : T(0));
     if (c == 0) {
@@ -107,82 +116,6 @@ struct StageCoef {
   T k1, k2, k3, k4;
 };
 
-// One RK stage for all three components; ST selects the update formula.
-// Stage update at one point (all three components).
-template <typename T, int ST>
-__device__ __forceinline__ void stage_point(const Geometry &g, const Coeffs<T> &co, const Fields<T> &F,
-                                            const StageCoef<T> &K, int forcing, const ForcingEval<T> &fe, int i, int j,
-                                            int k);
-
-// One RK stage; each thread updates the points (i, j, k) and (i, j, k + kh),
-// whose loads are independent, so twice as many are in flight per thread.
-template <typename T, int ST>
-__global__ void __launch_bounds__(128) stage_kernel(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
-                                                    int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot, int kh) {
-  if (forcing) {
-    fe.st = T(tr.get(sin_slot));
-    fe.ct = T(tr.get(sin_slot + 1));
-  }
-  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = 1 + blockIdx.z;
-  stage_point<T, ST>(g, co, F, K, forcing, fe, i, j, k);
-  if (k + kh < g.Es[2] - 1) stage_point<T, ST>(g, co, F, K, forcing, fe, i, j, k + kh);
-}
-
-template <typename T, int ST>
-__device__ __forceinline__ void stage_point(const Geometry &g, const Coeffs<T> &co, const Fields<T> &F,
-                                            const StageCoef<T> &K, int forcing, const ForcingEval<T> &fe, int i, int j,
-                                            int k) {
-  const long sy = g.sy(), sz = g.sz();
-  const long q = g.idx(i, j, k);
-  // The velocity set the right-hand side is computed from.
-  constexpr int in_set = (ST == kStageY2 || ST == kVelY2 || ST == kVelUStar) ? 0
-                         : (ST == kStageY3 || ST == kVelY3)                  ? 1
-                                                                             : 2;
-  const T *u = F.vel(in_set, 0), *v = F.vel(in_set, 1), *w = F.vel(in_set, 2);
-  const T *p = F.f[kP];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
-    T r = c == 0 ? rhs_u(u, v, w, q, sy, sz, co) : (c == 1 ? rhs_v(u, v, w, q, sy, sz, co) : rhs_w(u, v, w, q, sy, sz, co));
-    if (forcing) r = r + fe(c, i, j, k);
-    const long sc = c == 0 ? 1 : (c == 1 ? sy : sz);
-    if (ST == kStageY2) {
-      // src/Timestep.cpp:10-21: buf = u + a1 rhs - b grad p; buf2 = rhs   (k1 = a1, k3 = b)
-      const T gp = (ld(p, q) - ld(p, q - sc)) * co.oh[c];
-      F.vel(1, c)[q] = ld(F.vel(0, c), q) + K.k1 * r - K.k3 * gp;
-      F.vel(2, c)[q] = r;
-    } else if (ST == kStageY3) {
-      // src/Timestep.cpp:24-39: buf2 = buf + a1 rhs1 + a2 rhs2 - b grad p; u = a2 rhs2
-      const T gp = (ld(p, q) - ld(p, q - sc)) * co.oh[c];
-      const T r1 = F.vel(2, c)[q];
-      const T r2s = K.k2 * r;
-      F.vel(2, c)[q] = ld(F.vel(1, c), q) + K.k1 * r1 + r2s - K.k3 * gp;
-      F.vel(0, c)[q] = r2s;
-    } else if (ST == kStageUStar) {
-      // src/Timestep.cpp:42-54: u = buf2 - (a2 rhs2 held in u) + a3 rhs3 - b grad p   (k2 = a3, k3 = b)
-      const T gp = (ld(p, q) - ld(p, q - sc)) * co.oh[c];
-      const T r2s = -F.vel(0, c)[q];
-      F.vel(0, c)[q] = ld(F.vel(2, c), q) + r2s + K.k2 * r - K.k3 * gp;
-    } else if (ST == kVelY2) {
-      // src/TimestepVelocity.cpp:20-29: rhs_buffer = rhs; velocity_buffer = u + (dt a21) rhs
-      F.vel(2, c)[q] = r;
-      F.vel(1, c)[q] = ld(F.vel(0, c), q) + K.k1 * r;
-    } else if (ST == kVelY3) {
-      // src/TimestepVelocity.cpp:32-42 (k1 = dt, k2 = b1, k3 = a31, k4 = a32)
-      const T r1 = F.vel(2, c)[q];
-      const T uu = F.vel(0, c)[q];
-      F.vel(2, c)[q] = uu + K.k1 * (K.k2 * r1);
-      F.vel(0, c)[q] = uu + K.k1 * (K.k3 * r1 + K.k4 * r);
-    } else {
-      // src/TimestepVelocity.cpp:45-52: velocity_buffer = rhs_buffer + dt (b3 rhs)  (k1 = dt, k2 = b3)
-      const T r1 = F.vel(2, c)[q];
-      F.vel(1, c)[q] = r1 + K.k1 * (K.k2 * r);
-    }
-  }
-}
-
 // ---- 2.5D-tiled stage kernel ----
 //
 // A CTA owns a TX x TY tile of (i, j) and marches through kc planes of k. The
@@ -191,7 +124,9 @@ __device__ __forceinline__ void stage_point(const Geometry &g, const Coeffs<T> &
 // halo in x and y; plane k+2 is copied with cp.async while plane k is
 // computed. Every stencil neighbour of include/MomentumEquation.h then comes
 // from shared memory and each point costs about five global loads.
-constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kPL = kHX * kHY;
+// Tile rows hold kTX + 2 used elements at a pitch of kTX + 4, so every row
+// starts 16-byte aligned and is copied with 16-byte cp.async.
+constexpr int kTX = 32, kTY = 8, kHX = kTX + 4, kHY = kTY + 2, kPL = kHX * kHY;
 
 __device__ __forceinline__ void cp_async4_st(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -200,6 +135,10 @@ __device__ __forceinline__ void cp_async4_st(void *smem, const void *gmem) {
 __device__ __forceinline__ void cp_async8_st(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async16_st(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
 }
 // One element of T (4 or 8 bytes) into shared memory.
 template <typename T>
@@ -282,21 +221,22 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
   const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
   const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
   constexpr int nf = kUseP ? 4 : 3;
+  // A tile row starts at x = i0 - 1 = 32 * blockIdx.x (16-byte aligned, PX a
+  // multiple of 8) and is copied as kHX / kVec vectors of 16 bytes; vectors
+  // outside the box are zero-filled. Only the first kTX + 2 of a row are read.
+  constexpr int kVec = 16 / sizeof(T), kVecRow = kHX / kVec, kVecPlane = kVecRow * kHY;
   auto load_plane = [&](int kk) {
     if (kk >= 0 && kk < g.PZ) {
-      for (int e = threadIdx.x; e < kPL; e += kTX * kTY) {
-        const int hx = e % kHX, hy = e / kHX;
+      for (int e = threadIdx.x; e < kVecPlane * nf; e += kTX * kTY) {
+        const int f = e / kVecPlane, ev = e - f * kVecPlane;
+        const int hy = ev / kVecRow, hx = (ev - hy * kVecRow) * kVec;
         const int i = i0 - 1 + hx, j = j0 - 1 + hy;
-        const bool ok = i < g.PX && j < g.PY;
-        const long q = g.idx(i, j, kk);
-#pragma unroll
-        for (int f = 0; f < nf; ++f) {
-          T *d = &ring.f[f][kk & 3][e];
-          if (ok)
-            cp_async_elem(d, src[f] + q);
-          else
-            *d = T(0);
-        }
+        T *d = &ring.f[f][kk & 3][hy * kHX + hx];
+        const T *sp = f == 0 ? src[0] : (f == 1 ? src[1] : (f == 2 ? src[2] : src[3]));
+        if (i < g.PX && j < g.PY)
+          cp_async16_st(d, sp + g.idx(i, j, kk));
+        else
+          *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
     cp_commit();
@@ -307,8 +247,14 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
   const int i = i0 + tx, j = j0 + ty;
   const long sy = g.sy(), sz = g.sz();
   const Tap<T> base_tap{&ring, 0, (ty + 1) * kHX + tx + 1};
+  typename ForcingEval<T>::Axis fx{}, fy{}, fz{};
+  if (forcing) {
+    fx = fe.axis(0, min(i, fe.maxE - 1));
+    fy = fe.axis(1, min(j, fe.maxE - 1));
+  }
   for (int k = kbeg; k < kend; ++k) {
     load_plane(k + 2);
+    if (forcing) fz = fe.axis(2, k);
     cp_wait1();
     __syncthreads();
     Tap<T> A = base_tap;
@@ -318,7 +264,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
     for (int c = 0; c < 3; ++c) {
       if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
       T r = rhs_tap(c, A, co);
-      if (forcing) r = r + fe(c, i, j, k);
+      if (forcing) r = r + fe.eval(c, fx, fy, fz);
       T gp = T(0);
       if (kUseP) {
         const T pm = c == 0 ? A(3, -1, 0, 0) : (c == 1 ? A(3, 0, -1, 0) : A(3, 0, 0, -1));
