@@ -363,34 +363,48 @@ __device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row
 }
 
 // row[k] = Z_k (k < N) of the pair -> row[m] = X_m (m <= N) of both lines.
-// Thread t of the pair's N2 handles k in [t C, t C + C), C = N / (2 N2): the
-// even outputs directly, the odd ones as a running sum within the thread plus
-// an exclusive scan of the thread totals across the pair's lanes (the pair's
-// N2 threads are consecutive lanes of one warp).
+// The pair's N2 threads (consecutive lanes of one warp) own k = c N2 + t
+// (c < C = N / (2 N2)) for every bank-conflict-free pass over the row; the
+// running sum of the odd outputs is taken over contiguous blocks of C values
+// per thread, through a copy of D in the row at a padded index (k + k / C)
+// that makes those blocked accesses conflict-free too, and an exclusive scan
+// of the block totals across the lanes.
 template <typename T, int N1, int N2>
 __device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int t, typename Vec2<T>::type x1) {
   using T2 = typename Vec2<T>::type;
   constexpr int N = N1 * N2, C = N1 / 2;
   static_assert(N2 <= 32 && (N1 % 2) == 0, "pair within one warp");
+  auto pad = [](int k) { return k + k / C; };
 #pragma unroll
   for (int o = N2 / 2; o > 0; o >>= 1) {
     x1.x += __shfl_xor_sync(0xffffffffu, x1.x, o, N2);
     x1.y += __shfl_xor_sync(0xffffffffu, x1.y, o, N2);
   }
-  T2 ev[C], od[C];
-  T2 run = {T(0), T(0)};
-  const int kb = t * C;
+  // A: even outputs and the odd-output increments D_k (D_0 = 0), strided
+  T2 ev[C], dd[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int k = kb + c;
+    const int k = c * N2 + t;
     const T2 zk = row[k], zn = row[(N - k) & (N - 1)];
     ev[c].x = zk.x + zn.x;
     ev[c].y = zk.y + zn.y;
-    if (k > 0) {
-      run.x -= zk.y - zn.y;
-      run.y += zk.x - zn.x;
-    }
-    od[c] = run;
+    dd[c].x = k ? zn.y - zk.y : T(0);
+    dd[c].y = k ? zk.x - zn.x : T(0);
+  }
+  const T2 zh = row[N / 2];
+  __syncthreads();
+  // B: D to the padded scratch (the row is free now)
+#pragma unroll
+  for (int c = 0; c < C; ++c) row[pad(c * N2 + t)] = dd[c];
+  __syncthreads();
+  // C: blocked running sums, then the block offsets across the lanes
+  T2 run = {T(0), T(0)};
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const T2 d = row[pad(t * C + c)];
+    run.x += d.x;
+    run.y += d.y;
+    dd[c] = run;
   }
   T2 incl = run;
 #pragma unroll
@@ -406,16 +420,24 @@ __device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int
   excl.x = __shfl_up_sync(0xffffffffu, incl.x, 1, N2);
   excl.y = __shfl_up_sync(0xffffffffu, incl.y, 1, N2);
   if (t == 0) excl.x = excl.y = T(0);
-  const T2 zh = row[N / 2];
-  __syncthreads();  // every thread has read its Z values
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int k = kb + c;
-    row[2 * k] = ev[c];
     T2 o;
-    o.x = x1.x + (excl.x + od[c].x);
-    o.y = x1.y + (excl.y + od[c].y);
-    row[2 * k + 1] = o;
+    o.x = x1.x + (excl.x + dd[c].x);
+    o.y = x1.y + (excl.y + dd[c].y);
+    row[pad(t * C + c)] = o;
+  }
+  __syncthreads();
+  // D: the odd outputs back in the strided order
+#pragma unroll
+  for (int c = 0; c < C; ++c) dd[c] = row[pad(c * N2 + t)];
+  __syncthreads();
+  // E: X in natural order
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int k = c * N2 + t;
+    row[2 * k] = ev[c];
+    row[2 * k + 1] = dd[c];
   }
   if (t == N2 - 1) {
     T2 e;

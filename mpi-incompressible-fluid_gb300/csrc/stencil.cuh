@@ -74,9 +74,11 @@ void launch_neumann_flux(const Geometry &g, T *phi, int field_kind, TimeRef tr, 
                          cudaStream_t s, long long *launches);
 
 // p += phi everywhere; vel -= dt * grad(phi) on interior points (src/Timestep.cpp:66-81).
+// In float both updates round stochastically, drawn from the step time in
+// tr's slot 0 and `tag` (one per projection of a step).
 template <typename T>
-void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, cudaStream_t s,
-                    long long *launches);
+void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, TimeRef tr, unsigned tag,
+                    cudaStream_t s, long long *launches);
 
 // Reference layout (double, contiguous) <-> device layout (T, padded).
 template <typename T>

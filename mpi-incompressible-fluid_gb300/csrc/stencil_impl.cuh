@@ -9,6 +9,8 @@
 // solver.
 #pragma once
 
+#include <type_traits>
+
 #include <cmath>
 
 #include "analytic.cuh"
@@ -21,6 +23,57 @@ namespace {
 template <typename T>
 __device__ __forceinline__ T ld(const T *p, long q) {
   return __ldg(p + q);
+}
+
+// ---- stochastic rounding of FP32 state updates (mixed precision) ----
+//
+// A stage adds an increment of O(dt) to an O(1) velocity; rounded to the
+// nearest float the increment loses a biased share of its bits every time,
+// and with dt ~ h^2 that error grows with the number of stages. The state
+// updates of the float path therefore round stochastically: the exact sum
+// s + e (TwoSum, Knuth) is rounded to the neighbour of s on e's side with
+// probability |e| / ulp, so the rounding errors have mean zero and add up as a
+// random walk. The draw is a counter-based hash of the point, the component,
+// the stage and the step's time, so a run is deterministic.
+__device__ __forceinline__ unsigned sr_mix(unsigned x) {
+  // lowbias32 integer hash (public domain)
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// Per-launch salt from the step's time t_n (time slot 0) and a stage tag.
+__device__ __forceinline__ unsigned sr_salt(const TimeRef &tr, unsigned tag) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(tr.get(0));
+  return sr_mix((unsigned)b ^ (unsigned)(b >> 32) ^ (tag * 0x9e3779b9u));
+}
+
+__device__ __forceinline__ float add_sr(float b, float c, unsigned h) {
+  const float s = b + c;
+  const float bb = s - b;
+  const float e = (b - (s - bb)) + (c - bb);  // b + c == s + e exactly
+  if (e == 0.f || !isfinite(s)) return s;
+  int bits = __float_as_int(s);
+  if (s == 0.f)
+    bits = e > 0.f ? 1 : (int)0x80000001u;
+  else
+    bits += ((s > 0.f) == (e > 0.f)) ? 1 : -1;
+  const float nb = __int_as_float(bits);
+  const float u = (float)(h >> 8) * 5.9604644775390625e-8f;  // uniform in [0, 1), 24 bits
+  return fabsf(e) > u * fabsf(nb - s) ? nb : s;
+}
+
+// state + increment: stochastically rounded in float (h: the draw), exact
+// IEEE addition otherwise.
+template <typename T>
+__device__ __forceinline__ T state_add(T b, T c, unsigned h) {
+  if constexpr (std::is_same<T, float>::value)
+    return add_sr(b, c, h);
+  else
+    return b + c;
 }
 
 // include/MomentumEquation.h:42-116 (OPT_CPU_CACHE branch)
@@ -215,6 +268,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
     fe.st = T(tr.get(sin_slot));
     fe.ct = T(tr.get(sin_slot + 1));
   }
+  const unsigned salt = std::is_same<T, float>::value ? sr_salt(tr, 1u + ST) : 0u;
   const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
   const int i0 = 1 + blockIdx.x * kTX, j0 = 1 + blockIdx.y * kTY;
   const int zmax = g.Es[2] - 1;  // interior k < zmax
@@ -271,28 +325,32 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
         gp = (A(3, 0, 0, 0) - pm) * co.oh[c];
       }
       const T self = A(c, 0, 0, 0);  // the input set's own value at the point
+      // FP64 keeps the reference's expression order; the float path adds the
+      // increment to the state with stochastic rounding
+      constexpr bool kSR = std::is_same<T, float>::value;
+      const unsigned h = kSR ? sr_mix((unsigned)q ^ (salt + (unsigned)c * 0x85ebca6bu)) : 0u;
       if (ST == kStageY2) {
-        F.vel(1, c)[q] = self + K.k1 * r - K.k3 * gp;
+        F.vel(1, c)[q] = kSR ? state_add(self, K.k1 * r - K.k3 * gp, h) : self + K.k1 * r - K.k3 * gp;
         F.vel(2, c)[q] = r;
       } else if (ST == kStageY3) {
         const T r1 = F.vel(2, c)[q];
         const T r2s = K.k2 * r;
-        F.vel(2, c)[q] = self + K.k1 * r1 + r2s - K.k3 * gp;
+        F.vel(2, c)[q] = kSR ? state_add(self, K.k1 * r1 + r2s - K.k3 * gp, h) : self + K.k1 * r1 + r2s - K.k3 * gp;
         F.vel(0, c)[q] = r2s;
       } else if (ST == kStageUStar) {
         const T r2s = -F.vel(0, c)[q];
-        F.vel(0, c)[q] = self + r2s + K.k2 * r - K.k3 * gp;
+        F.vel(0, c)[q] = kSR ? state_add(self, r2s + K.k2 * r - K.k3 * gp, h) : self + r2s + K.k2 * r - K.k3 * gp;
       } else if (ST == kVelY2) {
         F.vel(2, c)[q] = r;
-        F.vel(1, c)[q] = self + K.k1 * r;
+        F.vel(1, c)[q] = kSR ? state_add(self, K.k1 * r, h) : self + K.k1 * r;
       } else if (ST == kVelY3) {
         const T r1 = F.vel(2, c)[q];
         const T uu = F.vel(0, c)[q];
-        F.vel(2, c)[q] = uu + K.k1 * (K.k2 * r1);
-        F.vel(0, c)[q] = uu + K.k1 * (K.k3 * r1 + K.k4 * r);
+        F.vel(2, c)[q] = kSR ? state_add(uu, K.k1 * (K.k2 * r1), h) : uu + K.k1 * (K.k2 * r1);
+        F.vel(0, c)[q] = kSR ? state_add(uu, K.k1 * (K.k3 * r1 + K.k4 * r), sr_mix(h)) : uu + K.k1 * (K.k3 * r1 + K.k4 * r);
       } else {
         const T r1 = F.vel(2, c)[q];
-        F.vel(1, c)[q] = r1 + K.k1 * (K.k2 * r);
+        F.vel(1, c)[q] = kSR ? state_add(r1, K.k1 * (K.k2 * r), h) : r1 + K.k1 * (K.k2 * r);
       }
     }
     __syncthreads();  // the next iteration refills the slot of plane k - 1
@@ -464,7 +522,8 @@ constexpr int kProjKZ = 4;
 
 template <typename T>
 __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict__ p, const T *__restrict__ phi,
-                                                      T *__restrict__ u, T *__restrict__ v, T *__restrict__ w, T dt) {
+                                                      T *__restrict__ u, T *__restrict__ v, T *__restrict__ w, T dt,
+                                                      TimeRef tr, unsigned tag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int kb = blockIdx.z * kProjKZ;
@@ -489,17 +548,21 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
       vv[c][r] = in ? vel[c][q] : T(0);
     }
   }
+  constexpr bool kSR = std::is_same<T, float>::value;
+  const unsigned salt = kSR ? sr_salt(tr, tag) : 0u;
 #pragma unroll
   for (int r = 0; r < kProjKZ; ++r) {
     const int k = kb + r;
     const long q = g.idx(i, j, k);
-    if (i < g.E[0] && j < g.E[1] && k < g.E[2]) p[q] = pv[r] + ph[r + 1];
+    const unsigned h = kSR ? sr_mix((unsigned)q ^ salt) : 0u;
+    if (i < g.E[0] && j < g.E[1] && k < g.E[2]) p[q] = kSR ? state_add(pv[r], ph[r + 1], h) : pv[r] + ph[r + 1];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
       const T below = c == 0 ? nb[0][r] : (c == 1 ? nb[1][r] : ph[r]);
       const T gp = (ph[r + 1] - below) * T(g.oh[c]);
-      vel[c][q] = vv[c][r] - gp * dt;
+      vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_mix(h + (unsigned)(c + 1) * 0x85ebca6bu))
+                      : vv[c][r] - gp * dt;
     }
   }
   (void)sc;
@@ -797,12 +860,12 @@ void launch_neumann_flux(const Geometry &g, T *phi, int field_kind, TimeRef tr, 
 }
 
 template <typename T>
-void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, cudaStream_t s,
-                    long long *launches) {
+void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, TimeRef tr, unsigned tag,
+                    cudaStream_t s, long long *launches) {
   const dim3 blk(32, 4, 1);
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
   const dim3 grid(cdiv(ni, 32), cdiv(g.Es[1], 4), cdiv(g.Es[2], kProjKZ));
-  project_kernel<T><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt));
+  project_kernel<T><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt), tr, tag);
   if (launches) ++*launches;
 }
 
@@ -884,7 +947,8 @@ void launch_nonfinite_check(const T *f, long n, int *flag, cudaStream_t s, long 
   template void launch_periodic_scalar<T>(const Geometry &, T *, cudaStream_t, long long *);                       \
   template void launch_divergence<T>(const Geometry &, T *, T *const[3], double, cudaStream_t, long long *);       \
   template void launch_neumann_flux<T>(const Geometry &, T *, int, TimeRef, int, int, cudaStream_t, long long *);  \
-  template void launch_project<T>(const Geometry &, T *, const T *, T *const[3], double, cudaStream_t, long long *); \
+  template void launch_project<T>(const Geometry &, T *, const T *, T *const[3], double, TimeRef, unsigned,      \
+                                  cudaStream_t, long long *);                                                     \
   template void launch_scatter<T>(const Geometry &, T *, const double *, int, int, int, cudaStream_t, long long *); \
   template void launch_gather<T>(const Geometry &, double *, const T *, int, int, int, cudaStream_t, long long *);  \
   template void launch_set_exact<T>(const Geometry &, T *, int, int, double, cudaStream_t, long long *);           \

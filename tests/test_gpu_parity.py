@@ -215,12 +215,14 @@ def test_poisson_solution_satisfies_discrete_laplacian(mifgpu_lib, cuda_device):
 
 
 @pytest.mark.parametrize("shape,periodic", [
-    ((33, 65, 129), (False, False, False)),   # DCT-I lengths 64, 128, 256 (register path)
-    ((257, 17, 33), (False, False, False)),   # 512
-    ((513, 9, 17), (False, False, False)),    # 1024
+    # a DCT-I line of n points runs on the register path as a length n-1 transform
+    ((33, 65, 129), (False, False, False)),   # DCT-I: shared-memory 64 / register 64, 128 (z fused)
+    ((257, 17, 33), (False, False, False)),   # register 256
+    ((513, 9, 17), (False, False, False)),    # register 512
+    ((1025, 9, 5), (False, False, False)),    # register 1024
     ((65, 129, 33), (True, True, True)),      # real DFT lengths 64, 128, 32 (32: shared-memory path)
-    ((257, 65, 513), (True, False, True)),    # channel-like: 256 / DCT 128 / 512
-    ((17, 513, 9), (False, False, False)),    # 1024 along the strided y axis
+    ((257, 65, 513), (True, False, True)),    # channel-like: real DFT 256 / DCT 64 / real DFT 512
+    ((17, 513, 9), (False, False, False)),    # register 512 along the strided y axis
 ])
 def test_mixed_poisson_matches_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, periodic):
     """Mixed-precision Poisson solve (register FFT for power-of-two lengths)
