@@ -12,6 +12,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mifgpu.h"
@@ -121,8 +122,16 @@ void field_extent(const Geometry &g, int id, int e[3]) {
   }
 }
 
+// Time factors of the analytic families at the slot's four times.
+void slot_factors(double *s, int kind, double Re) {
+  for (int q = 0; q < 4; ++q) {
+    s[kSlotFactor + q] = family_time_factor(kind, 0, s[q], Re);
+    s[kSlotFactor + 4 + q] = family_time_factor(kind, 1, s[q], Re);
+  }
+}
+
 // Times of one projection step, computed as src/Timestep.cpp:97-104 does.
-void projection_slot(double t_n, double dt, double *s) {
+void projection_slot(double t_n, double dt, int kind, double Re, double *s) {
   const double dt_1 = 64.0 / 120.0 * dt;
   const double time_1 = t_n + dt_1;
   const double dt_2 = 16.0 / 120.0 * dt;
@@ -138,10 +147,11 @@ void projection_slot(double t_n, double dt, double *s) {
   s[7] = std::cos(time_1);
   s[8] = std::sin(time_2);
   s[9] = std::cos(time_2);
+  slot_factors(s, kind, Re);
 }
 
 // Times of one velocity-only step, src/TimestepVelocity.cpp:63-65.
-void velocity_slot(double t_n, double dt, double *s) {
+void velocity_slot(double t_n, double dt, int kind, double Re, double *s) {
   const double c2 = (8.0 / 15.0), c3 = (2.0 / 3.0);
   const double time_1 = t_n + c2 * dt;
   const double time_2 = t_n + c3 * dt;
@@ -156,6 +166,7 @@ void velocity_slot(double t_n, double dt, double *s) {
   s[7] = std::cos(time_1);
   s[8] = std::sin(time_2);
   s[9] = std::cos(time_2);
+  slot_factors(s, kind, Re);
 }
 
 enum { kVariantProjection = 0, kVariantNhn = 1, kVariantVelocity = 2 };
@@ -181,6 +192,8 @@ struct Impl final : ImplBase {
   double *staging = nullptr;
   size_t staging_elems = 0;
   T *grad_block = nullptr;  // three fields for the pressure-gradient norm
+  double *face_tab = nullptr;  // float path: the families' face data in double
+  FaceTables ftabs{};
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   long long graph_launches[3][2] = {{0, 0}, {0, 0}, {0, 0}};
@@ -221,6 +234,7 @@ struct Impl final : ImplBase {
     cudaFree(acc);
     cudaFree(staging);
     cudaFree(grad_block);
+    cudaFree(face_tab);
     cudaFree(adj_block);
     cudaFree(ckpt_block);
     cudaFree(snap_block);
@@ -254,11 +268,40 @@ struct Impl final : ImplBase {
         }
     CK(cudaMalloc(&ftab, sizeof(T) * tab.size()));
     CK(cudaMemcpy(ftab, tab.data(), sizeof(T) * tab.size(), cudaMemcpyHostToDevice));
+    if (int rc = init_face_tables(ctx)) return rc;
     CK(cudaMalloc(&step_ctr, sizeof(int)));
     CK(cudaMemset(step_ctr, 0, sizeof(int)));
     CK(cudaMalloc(&acc, sizeof(double) * 16));
     CK(alloc_slots());
     CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    return MIFGPU_OK;
+  }
+
+  // Float path: the Dirichlet data of the analytic family is a spatial field
+  // times a factor of t, so its faces are evaluated once in double and every
+  // boundary fill is one multiplication and one rounding (the working-precision
+  // evaluation of exp/sin/cos products cost several ulp of |u| per fill).
+  int init_face_tables(mifgpu_ctx *ctx) {
+    const int kind = ctx->prm.boundary_kind;
+    if (!std::is_same<T, float>::value || kind == 0 || (g.periodic[0] && g.periodic[1] && g.periodic[2]))
+      return MIFGPU_OK;
+    long n = 0;
+    for (int fn = 0; fn < 2; ++fn)
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) {
+          if (g.periodic[d]) continue;
+          const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+          for (int sd = 0; sd < 2; ++sd) {
+            ftabs.off[fn][c][d][sd] = n;
+            n += (long)g.ext(c, a) * g.ext(c, b);
+          }
+        }
+    if (cudaMalloc(&face_tab, sizeof(double) * n) != cudaSuccess)
+      return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the boundary face tables failed");
+    total_bytes += sizeof(double) * n;
+    ftabs.tab = face_tab;
+    for (int fn = 0; fn < 2; ++fn) launch_face_tables(g, kind, fn, face_tab, ftabs, nullptr);
+    CK(cudaDeviceSynchronize());
     return MIFGPU_OK;
   }
 
@@ -362,7 +405,7 @@ struct Impl final : ImplBase {
   void enqueue_bc(mifgpu_ctx *ctx, cudaStream_t s, int set, int t_slot, long long *cnt) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
     mark(MIFGPU_PROF_BOUNDARY, s);
-    launch_apply_bc<T>(g, vel, ctx->prm.boundary_kind, 0, tref(), t_slot, s, cnt);
+    launch_apply_bc<T>(g, vel, ctx->prm.boundary_kind, 0, tref(), t_slot, ftabs, s, cnt);
   }
 
   void enqueue_project(cudaStream_t s, int set, double dt, unsigned tag, long long *cnt) {
@@ -439,7 +482,7 @@ struct Impl final : ImplBase {
 
   int profile_step(mifgpu_ctx *ctx, double t_n, int reps, double *ms) override {
     double sl[kSlotSize];
-    projection_slot(t_n, g.dt, sl);
+    projection_slot(t_n, g.dt, ctx->prm.boundary_kind, g.Re, sl);
     CK(cudaMemcpyAsync(slots, sl, sizeof(sl), cudaMemcpyHostToDevice, ctx->stream));
     for (int c = 0; c < MIFGPU_PROF_CLASSES; ++c) ms[c] = 0.0;
     for (int r = 0; r < reps; ++r) {
@@ -463,8 +506,9 @@ struct Impl final : ImplBase {
 
   int write_single_slot(mifgpu_ctx *ctx, double t) {
     double s[kSlotSize];
-    projection_slot(t, g.dt, s);
+    projection_slot(t, g.dt, ctx->prm.boundary_kind, g.Re, s);
     s[1] = s[2] = s[3] = t;  // sub-step calls use their own time in every slot
+    slot_factors(s, ctx->prm.boundary_kind, g.Re);
     CK(cudaMemcpyAsync(slots, s, sizeof(s), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(step_ctr, 0, sizeof(int), ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -516,7 +560,7 @@ struct Impl final : ImplBase {
     launch_pressure_errors<T>(g, F.f[kP], kind, t, acc + 3, ctx->stream, &ctx->launches);
     launch_pressure_gradient<T>(g, gv, F.f[kP], ctx->stream, &ctx->launches);
     if (int rc = write_single_slot(ctx, t)) return rc;
-    launch_apply_bc<T>(g, gv, kind, 1, tref(), 0, ctx->stream, &ctx->launches);
+    launch_apply_bc<T>(g, gv, kind, 1, tref(), 0, ftabs, ctx->stream, &ctx->launches);
     launch_velocity_errors<T>(g, gv, kind, 1, t, acc + 6, ctx->stream, &ctx->launches);
     double h[9];
     CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
@@ -644,7 +688,8 @@ struct Impl final : ImplBase {
     cudaStream_t s = ctx->stream;
     long long *cnt = &ctx->launches;
     std::vector<double> sl((size_t)kSlotSize * N);
-    for (int n = 0; n < N; ++n) projection_slot(req.t0 + n * g.dt, g.dt, sl.data() + (size_t)kSlotSize * n);
+    for (int n = 0; n < N; ++n)
+      projection_slot(req.t0 + n * g.dt, g.dt, ctx->prm.boundary_kind, g.Re, sl.data() + (size_t)kSlotSize * n);
     T *set0 = F.vel(0, 0), *set1 = F.vel(1, 0), *set2 = F.vel(2, 0), *p = F.f[kP];
     auto ck = [&](int seg) { return ckpt_block + (size_t)4 * seg * field_elems; };
     auto sn = [&](int m) { return snap_block + (size_t)9 * m * field_elems; };
@@ -895,7 +940,7 @@ int mifgpu_set_exact_pressure(mifgpu_ctx *ctx, double t) {
 int mifgpu_timestep(mifgpu_ctx *ctx, double t_n) {
   if (!ctx) return MIFGPU_EINVAL;
   double s[kSlotSize];
-  projection_slot(t_n, ctx->g.dt, s);
+  projection_slot(t_n, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s);
   return ctx->impl->step(ctx, kVariantProjection, s, 1);
 }
 
@@ -903,7 +948,8 @@ int mifgpu_run(mifgpu_ctx *ctx, double t0, int nsteps) {
   if (!ctx || nsteps < 0) return MIFGPU_EINVAL;
   if (nsteps == 0) return MIFGPU_OK;
   std::vector<double> s((size_t)kSlotSize * nsteps);
-  for (int n = 0; n < nsteps; ++n) projection_slot(t0 + n * ctx->g.dt, ctx->g.dt, s.data() + (size_t)kSlotSize * n);
+  for (int n = 0; n < nsteps; ++n)
+    projection_slot(t0 + n * ctx->g.dt, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s.data() + (size_t)kSlotSize * n);
   return ctx->impl->step(ctx, kVariantProjection, s.data(), nsteps);
 }
 
@@ -924,14 +970,14 @@ int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n) {
   if (ctx->g.periodic[0] || ctx->g.periodic[1] || ctx->g.periodic[2])
     return fail(ctx, MIFGPU_ENOTSUP, "non-homogeneous Neumann data needs every axis non-periodic");
   double s[kSlotSize];
-  projection_slot(t_n, ctx->g.dt, s);
+  projection_slot(t_n, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s);
   return ctx->impl->step(ctx, kVariantNhn, s, 1);
 }
 
 int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n) {
   if (!ctx) return MIFGPU_EINVAL;
   double s[kSlotSize];
-  velocity_slot(t_n, ctx->g.dt, s);
+  velocity_slot(t_n, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s);
   if (int rc = ctx->impl->step(ctx, kVariantVelocity, s, 1)) return rc;
   ctx->impl->swap_sets();  // src/TimestepVelocity.cpp:89
   return MIFGPU_OK;

@@ -33,12 +33,27 @@ struct ForcingTables {
 // replayed step after step: slot s of step n is slots[n * kSlotSize + s] with
 // n = *step. Layout of one step's slot (doubles):
 //   0 t_n, 1 time_1, 2 time_2, 3 final time,
-//   4/5 sin/cos(t_n), 6/7 sin/cos(time_1), 8/9 sin/cos(time_2)
-constexpr int kSlotSize = 10;
+//   4/5 sin/cos(t_n), 6/7 sin/cos(time_1), 8/9 sin/cos(time_2),
+//   10..13 the velocity family's time factor at times 0..3,
+//   14..17 the pressure-gradient family's time factor at times 0..3
+// (both families are a spatial field times a factor of t; see FaceTables).
+constexpr int kSlotSize = 18;
+constexpr int kSlotFactor = 10;
 struct TimeRef {
   const double *slots;
   const int *step;
   __device__ __forceinline__ double get(int s) const { return slots[(long)(*step) * kSlotSize + s]; }
+};
+
+// Dirichlet face data of the analytic families, precomputed in double at a
+// unit time for the float path: value(x, t) = tab[...](x) * factor(t), with the
+// factor in the time slots. off[fn][c][d][s] is the start of the table of
+// family fn (0 velocity, 1 pressure gradient), component c, faces normal to
+// axis d, side s; the face point (pa, pb) (the two other axes, in order) is at
+// pa + ext(c, a) * pb. A null tab means: evaluate in the working precision.
+struct FaceTables {
+  const double *tab = nullptr;
+  long off[2][3][3][2] = {};
 };
 
 template <typename T>
@@ -57,7 +72,16 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
 // periodic copies, on velocity set `set` (src/VelocityTensor.cpp:36-233).
 template <typename T>
 void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn, TimeRef tr, int t_slot,
-                     cudaStream_t s, long long *launches);
+                     const FaceTables &ft, cudaStream_t s, long long *launches);
+
+// Fills the face tables of family fn (see FaceTables) in double.
+void launch_face_tables(const Geometry &g, int field_kind, int fn, double *tab, const FaceTables &ft,
+                        cudaStream_t s);
+
+// Time factor of family fn (0 velocity, 1 pressure gradient) at time t, and
+// the unit time at which the tables are evaluated.
+double family_time_factor(int field_kind, int fn, double t, double Re);
+double family_unit_time(int field_kind);
 
 // Periodic ghost copy of a pressure-shaped field (src/StaggeredTensor.cpp:221-257).
 template <typename T>

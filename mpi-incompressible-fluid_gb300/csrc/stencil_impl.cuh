@@ -406,9 +406,11 @@ __device__ TE face_value(const Geometry &g, int c, int d, int s, const long *pt,
 // point is written once, by the face the reference writes last (order
 // z_min, z_max, y_min, y_max, x_min, x_max).
 template <typename T>
-__global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int fn, TimeRef tr, int t_slot) {
+__global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int fn, TimeRef tr, int t_slot,
+                                FaceTables ft) {
   const int c = blockIdx.z / 3, d = blockIdx.z % 3;
   const double t = tr.get(t_slot);
+  const double factor = ft.tab ? tr.get(kSlotFactor + 4 * fn + t_slot) : 0.0;
   if (g.periodic[d]) return;
   const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
   const long pa = blockIdx.x * blockDim.x + threadIdx.x;
@@ -424,7 +426,8 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
     for (int d2 = 0; d2 < d; ++d2)
       if (!g.periodic[d2] && (pt[d2] == 0 || pt[d2] == g.ext(c, d2) - 1)) later = true;
     if (later) continue;
-    const T val = T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
+    const T val = ft.tab ? T(ft.tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor)
+                         : T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
     f[g.idx(pt[0], pt[1], pt[2])] = val;
   }
 }
@@ -813,13 +816,13 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
 
 template <typename T>
 void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn, TimeRef tr, int t_slot,
-                     cudaStream_t s, long long *launches) {
+                     const FaceTables &ft, cudaStream_t s, long long *launches) {
   const dim3 blk(32, 8, 1);
   int mx = 0;
   for (int d = 0; d < 3; ++d) mx = mx > g.Es[d] ? mx : g.Es[d];
   if (!(g.periodic[0] && g.periodic[1] && g.periodic[2])) {
     const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 9);
-    bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot);
+    bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft);
     if (launches) ++*launches;
   }
   for (int d = 0; d < 3; ++d) {
@@ -829,6 +832,46 @@ void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn
     if (launches) ++*launches;
   }
 }
+
+// Precision-independent pieces: compiled in one translation unit only.
+#ifdef MIFGPU_STENCIL_SHARED
+__global__ void face_table_kernel(Geometry g, int kind, int fn, double tu, double *tab, FaceTables ft) {
+  const int c = blockIdx.z / 3, d = blockIdx.z % 3;
+  if (g.periodic[d]) return;
+  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+  const long pa = blockIdx.x * blockDim.x + threadIdx.x;
+  const long pb = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) return;
+  for (int s = 0; s < 2; ++s) {
+    long pt[3];
+    pt[a] = pa;
+    pt[b] = pb;
+    pt[d] = s == 0 ? 0 : g.ext(c, d) - 1;
+    tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] = face_value<double>(g, c, d, s, pt, kind, fn, tu);
+  }
+}
+
+void launch_face_tables(const Geometry &g, int field_kind, int fn, double *tab, const FaceTables &ft,
+                        cudaStream_t s) {
+  int mx = 0;
+  for (int d = 0; d < 3; ++d) mx = mx > g.Es[d] ? mx : g.Es[d];
+  face_table_kernel<<<dim3(cdiv(mx, 32), cdiv(mx, 8), 9), dim3(32, 8, 1), 0, s>>>(g, field_kind, fn,
+                                                                                   family_unit_time(field_kind), tab,
+                                                                                   ft);
+}
+
+// SINCOS: sin t for both families; ETHIER: exp(-d^2 t / Re) for the velocity
+// and its square for the pressure gradient (generators/manufsol.py:35-72).
+double family_time_factor(int field_kind, int fn, double t, double Re) {
+  if (field_kind == kFieldSincos) return std::sin(t);
+  if (field_kind == kFieldEthier) {
+    const double d = 1.57079632679489661923;
+    return std::exp(-(fn == 0 ? 1.0 : 2.0) * d * d * t / Re);
+  }
+  return 0.0;
+}
+double family_unit_time(int field_kind) { return field_kind == kFieldSincos ? 1.57079632679489661923 : 0.0; }
+#endif  // MIFGPU_STENCIL_SHARED
 
 template <typename T>
 void launch_periodic_scalar(const Geometry &g, T *f, cudaStream_t s, long long *launches) {
@@ -943,7 +986,8 @@ void launch_nonfinite_check(const T *f, long n, int *flag, cudaStream_t s, long 
 #define MIFGPU_INSTANTIATE(T)                                                                                        \
   template void launch_stage<T>(const Geometry &, const Fields<T> &, StageKind, const StageScalars<T> &,             \
                                 const ForcingTables<T> &, int, TimeRef, cudaStream_t, long long *);                  \
-  template void launch_apply_bc<T>(const Geometry &, T *const[3], int, int, TimeRef, int, cudaStream_t, long long *); \
+  template void launch_apply_bc<T>(const Geometry &, T *const[3], int, int, TimeRef, int, const FaceTables &,     \
+                                   cudaStream_t, long long *);                                                    \
   template void launch_periodic_scalar<T>(const Geometry &, T *, cudaStream_t, long long *);                       \
   template void launch_divergence<T>(const Geometry &, T *, T *const[3], double, cudaStream_t, long long *);       \
   template void launch_neumann_flux<T>(const Geometry &, T *, int, TimeRef, int, int, cudaStream_t, long long *);  \
