@@ -33,8 +33,9 @@ __device__ __forceinline__ T ld(const T *p, long q) {
 // updates of the float path therefore round stochastically: the exact sum
 // s + e (TwoSum, Knuth) is rounded to the neighbour of s on e's side with
 // probability |e| / ulp, so the rounding errors have mean zero and add up as a
-// random walk. The draw is a counter-based hash of the point, the component,
-// the stage and the step's time, so a run is deterministic.
+// random walk. The draws come from a counter-based hash of the point, the
+// stage and the step's time (ten bits per update: a probability resolution of
+// 1/1024 ulp), so a run is deterministic.
 __device__ __forceinline__ unsigned sr_mix(unsigned x) {
   // lowbias32 integer hash (public domain)
   x ^= x >> 16;
@@ -51,27 +52,30 @@ __device__ __forceinline__ unsigned sr_salt(const TimeRef &tr, unsigned tag) {
   return sr_mix((unsigned)b ^ (unsigned)(b >> 32) ^ (tag * 0x9e3779b9u));
 }
 
-__device__ __forceinline__ float add_sr(float b, float c, unsigned h) {
+// b + c rounded stochastically; r in [0, 1) is the draw. The neighbour of s on
+// e's side is one unit in the last place away from s: +1 in the bit pattern
+// when s and e have the same sign, -1 otherwise. Rounding to the neighbour
+// with probability |e| / ulp keeps the expected result b + c.
+__device__ __forceinline__ float add_sr(float b, float c, float r) {
   const float s = b + c;
   const float bb = s - b;
   const float e = (b - (s - bb)) + (c - bb);  // b + c == s + e exactly
-  if (e == 0.f || !isfinite(s)) return s;
-  int bits = __float_as_int(s);
-  if (s == 0.f)
-    bits = e > 0.f ? 1 : (int)0x80000001u;
-  else
-    bits += ((s > 0.f) == (e > 0.f)) ? 1 : -1;
-  const float nb = __int_as_float(bits);
-  const float u = (float)(h >> 8) * 5.9604644775390625e-8f;  // uniform in [0, 1), 24 bits
-  return fabsf(e) > u * fabsf(nb - s) ? nb : s;
+  const int sb = __float_as_int(s);
+  const float nb = __int_as_float(sb + (((sb ^ __float_as_int(e)) >> 31) | 1));
+  return (s != 0.f && fabsf(e) > r * fabsf(nb - s)) ? nb : s;
+}
+
+// Ten-bit uniform draw number `slot` (0..2) from a 32-bit hash.
+__device__ __forceinline__ float sr_draw(unsigned h, int slot) {
+  return (float)((h >> (10 * slot)) & 1023u) * (1.0f / 1024.0f);
 }
 
 // state + increment: stochastically rounded in float (h: the draw), exact
 // IEEE addition otherwise.
 template <typename T>
-__device__ __forceinline__ T state_add(T b, T c, unsigned h) {
+__device__ __forceinline__ T state_add(T b, T c, float r) {
   if constexpr (std::is_same<T, float>::value)
-    return add_sr(b, c, h);
+    return add_sr(b, c, r);
   else
     return b + c;
 }
@@ -314,6 +318,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
     Tap<T> A = base_tap;
     A.k = k;
     const long q = g.idx(i, j, k);
+    const unsigned hq = std::is_same<T, float>::value ? sr_mix((unsigned)q ^ salt) : 0u;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
@@ -328,7 +333,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
       // FP64 keeps the reference's expression order; the float path adds the
       // increment to the state with stochastic rounding
       constexpr bool kSR = std::is_same<T, float>::value;
-      const unsigned h = kSR ? sr_mix((unsigned)q ^ (salt + (unsigned)c * 0x85ebca6bu)) : 0u;
+      const float h = kSR ? sr_draw(hq, c) : 0.f;
       if (ST == kStageY2) {
         F.vel(1, c)[q] = kSR ? state_add(self, K.k1 * r - K.k3 * gp, h) : self + K.k1 * r - K.k3 * gp;
         F.vel(2, c)[q] = r;
@@ -347,7 +352,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
         const T r1 = F.vel(2, c)[q];
         const T uu = F.vel(0, c)[q];
         F.vel(2, c)[q] = kSR ? state_add(uu, K.k1 * (K.k2 * r1), h) : uu + K.k1 * (K.k2 * r1);
-        F.vel(0, c)[q] = kSR ? state_add(uu, K.k1 * (K.k3 * r1 + K.k4 * r), sr_mix(h)) : uu + K.k1 * (K.k3 * r1 + K.k4 * r);
+        F.vel(0, c)[q] = kSR ? state_add(uu, K.k1 * (K.k3 * r1 + K.k4 * r), 1.0f - h) : uu + K.k1 * (K.k3 * r1 + K.k4 * r);
       } else {
         const T r1 = F.vel(2, c)[q];
         F.vel(1, c)[q] = kSR ? state_add(r1, K.k1 * (K.k2 * r), h) : r1 + K.k1 * (K.k2 * r);
@@ -558,14 +563,15 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
     const int k = kb + r;
     const long q = g.idx(i, j, k);
     const unsigned h = kSR ? sr_mix((unsigned)q ^ salt) : 0u;
-    if (i < g.E[0] && j < g.E[1] && k < g.E[2]) p[q] = kSR ? state_add(pv[r], ph[r + 1], h) : pv[r] + ph[r + 1];
+    const unsigned h2 = kSR ? sr_mix(h) : 0u;
+    if (i < g.E[0] && j < g.E[1] && k < g.E[2])
+      p[q] = kSR ? state_add(pv[r], ph[r + 1], sr_draw(h2, 0)) : pv[r] + ph[r + 1];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
       const T below = c == 0 ? nb[0][r] : (c == 1 ? nb[1][r] : ph[r]);
       const T gp = (ph[r + 1] - below) * T(g.oh[c]);
-      vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_mix(h + (unsigned)(c + 1) * 0x85ebca6bu))
-                      : vv[c][r] - gp * dt;
+      vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_draw(h, c)) : vv[c][r] - gp * dt;
     }
   }
   (void)sc;
