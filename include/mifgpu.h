@@ -102,10 +102,10 @@ int mifgpu_field_extent(const mifgpu_ctx *ctx, int field, long out[3]);
 /* Host <-> device copies of one field in the reference layout (double).
  * upload is asynchronous on the context's stream: the host buffer must stay
  * valid until the next synchronising call. download returns after the data
- * has landed in `host`. A pinned host buffer (and any host buffer where the
- * GPU reads pageable memory through the host page tables, as on Grace over
- * NVLink-C2C) is read or written by the layout kernels in place; other
- * buffers travel through a device staging copy. */
+ * has landed in `host`. The data travels as one DMA copy into a device
+ * staging buffer and one layout kernel (measured on GB300: ~200 GB/s for
+ * pinned and pageable buffers alike; kernels reading host memory directly
+ * over NVLink-C2C were ~10% slower). */
 int mifgpu_upload(mifgpu_ctx *ctx, int field, const double *host);
 int mifgpu_download(mifgpu_ctx *ctx, int field, double *host);
 

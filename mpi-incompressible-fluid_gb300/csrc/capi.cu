@@ -63,7 +63,6 @@ struct ImplBase {
 struct mifgpu_ctx {
   mifgpu_params prm{};
   int device = 0;
-  int pageable_access = 0;  // the device reads pageable host memory through the host page tables
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   Geometry g{};
@@ -88,29 +87,6 @@ int cuda_fail(mifgpu_ctx *ctx, cudaError_t e, const char *where) {
     cudaError_t e_ = (call);                                  \
     if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
   } while (0)
-
-// An address the kernels can use for the caller's buffer p, or null when it
-// has to travel through a staged copy: pinned (UVA-mapped) host memory, this
-// device's or managed memory, or any host memory when the device reads
-// pageable memory through the host page tables (NVLink-C2C on Grace). The
-// scatter/gather kernels then read or write it directly, in one pass.
-const void *direct_view(const mifgpu_ctx *ctx, const void *p) {
-  cudaPointerAttributes at{};
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  switch (at.type) {
-    case cudaMemoryTypeHost:
-      return at.devicePointer;
-    case cudaMemoryTypeDevice:
-      return at.device == ctx->device ? p : nullptr;
-    case cudaMemoryTypeManaged:
-      return p;
-    default:
-      return ctx->pageable_access ? p : nullptr;
-  }
-}
 
 // Extents of field id in the reference layout.
 void field_extent(const Geometry &g, int id, int e[3]) {
@@ -345,12 +321,6 @@ struct Impl final : ImplBase {
   int upload(mifgpu_ctx *ctx, int id, const double *host) override {
     int e[3];
     field_extent(g, id, e);
-    if (const void *src = direct_view(ctx, host)) {
-      launch_scatter<T>(g, F.f[id], static_cast<const double *>(src), e[0], e[1], e[2], ctx->stream,
-                        &ctx->launches);
-      CK(cudaGetLastError());
-      return MIFGPU_OK;
-    }
     if (int rc = ensure_staging(ctx)) return rc;
     const size_t n = (size_t)e[0] * e[1] * e[2];
     CK(cudaMemcpyAsync(staging, host, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -362,13 +332,6 @@ struct Impl final : ImplBase {
   int download(mifgpu_ctx *ctx, int id, double *host) override {
     int e[3];
     field_extent(g, id, e);
-    if (const void *dst = direct_view(ctx, host)) {
-      launch_gather<T>(g, static_cast<double *>(const_cast<void *>(dst)), F.f[id], e[0], e[1], e[2], ctx->stream,
-                       &ctx->launches);
-      CK(cudaGetLastError());
-      CK(cudaStreamSynchronize(ctx->stream));
-      return MIFGPU_OK;
-    }
     if (int rc = ensure_staging(ctx)) return rc;
     const size_t n = (size_t)e[0] * e[1] * e[2];
     launch_gather<T>(g, staging, F.f[id], e[0], e[1], e[2], ctx->stream, &ctx->launches);
@@ -862,11 +825,6 @@ int mifgpu_create(const mifgpu_params *p, mifgpu_ctx **out) {
   g.Re = p->Re;
   g.dt = p->dt;
   if (cudaGetDevice(&ctx->device) != cudaSuccess) return fail(nullptr, MIFGPU_ECUDA, "no CUDA device");
-  if (cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    ctx->pageable_access = 0;
-  }
   if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) return MIFGPU_ECUDA;
   ctx->stream = ctx->own_stream;
   if (p->precision == MIFGPU_FP64)
