@@ -47,10 +47,7 @@ struct PoissonSolver {
   // In place on the owner block of phi: rhs in, solution out (no periodic refresh).
   // `mark`, when set, is called with the sweep id (0 x-forward, 1 y-forward,
   // 2 z forward+eigen+inverse, 3 y-inverse, 4 x-inverse) before each launch.
-  // When `vel` is given, the x-forward sweep computes the right-hand side
-  // div(vel)/dt itself and phi's previous contents are not read.
-  int solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark = nullptr,
-            T *const *vel = nullptr, double dt = 1.0);
+  int solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark = nullptr);
 };
 
 }  // namespace mifgpu

@@ -71,13 +71,6 @@ struct LineArgs {
   // kModeFwdEigInv only: 1/(lambda_x + lambda_y + lambda_z) on the owner block,
   // x fastest, computed in double at set-up, zero mode 0.
   const T *eig;
-  // x-forward sweep fused with the right-hand side: when du is set the line
-  // values are div(u)/dt at the owner points (src/PressureEquation.cpp:59-61,
-  // include/VelocityDivergence.h:9-20) instead of data[].
-  const T *du, *dv, *dw;
-  long vsy, vsz;
-  T doh[3];
-  T inv_dt;
 };
 
 // Per-CTA line table: global offset of each line's first element (-1 past the
@@ -106,12 +99,6 @@ __device__ void fill_line_table(LineTable &t, const LineArgs<T> &a, long line0, 
 
 template <typename T>
 __device__ __forceinline__ T line_value(const LineArgs<T> &a, long q) {
-  if (a.du) {
-    const T du = (__ldg(a.du + q + 1) - __ldg(a.du + q)) * a.doh[0];
-    const T dv = (__ldg(a.dv + q + a.vsy) - __ldg(a.dv + q)) * a.doh[1];
-    const T dw = (__ldg(a.dw + q + a.vsz) - __ldg(a.dw + q)) * a.doh[2];
-    return (du + dv + dw) * a.inv_dt;
-  }
   return a.data[q];
 }
 
@@ -504,56 +491,30 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
   const int nl = 2 * a.P;
 
   fill_line_table(table, a, line0, total);
-  if (a.du) {
-    // x-forward fused with the divergence: the CTA's nl x n elements as one
-    // flat range, eight per thread per round so their 48 loads are in flight
-    // together (consecutive threads on consecutive x: coalesced).
-    const int cnt = nl * n;
-    constexpr int U = 8;
-    for (int e0 = threadIdx.x; e0 < cnt; e0 += U * blockDim.x) {
-      T v[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int e = e0 + u * blockDim.x;
-        v[u] = T(0);
-        if (e < cnt) {
-          const int l = e / n, m = e - l * n;
-          const long off = table.off[l];
-          if (off >= 0) v[u] = line_value(a, off + m);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int e = e0 + u * blockDim.x;
-        if (e < cnt) {
-          const int l = e / n, m = e - l * n;
-          reinterpret_cast<T *>(s + (l >> 1) * ROW + m)[l & 1] = v[u];
-        }
-      }
-    }
-  } else if (a.line_fast) {
-    // Strided lines: consecutive threads on consecutive lines (consecutive
-    // addresses), copied asynchronously.
-    const int cnt = nl * n;
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-      const int m = e >> a.lg_lines, l = e & (nl - 1);
-      T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW + m) + (l & 1);
-      const long off = table.off[l];
-      if (off >= 0)
-        cp_async4(dst, a.data + off + (long)m * a.se);
-      else
-        *dst = T(0);
+  if (a.line_fast) {
+    // Strided lines: consecutive threads own consecutive lines (consecutive
+    // addresses at each m); each thread keeps its line and walks m.
+    const int l = threadIdx.x & (nl - 1);
+    const long off = table.off[l];
+    T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
+    const int ms = blockDim.x >> a.lg_lines;
+    if (off >= 0) {
+      const T *src0 = a.data + off;
+      for (int m = threadIdx.x >> a.lg_lines; m < n; m += ms) cp_async4(dst + 2 * m, src0 + (long)m * a.se);
+    } else {
+      for (int m = threadIdx.x >> a.lg_lines; m < n; m += ms) dst[2 * m] = T(0);
     }
   } else {
-    // Contiguous x lines, copied asynchronously row by row.
-    for (int l = 0; l < nl; ++l) {
+    // Contiguous x lines: one warp per line, lanes on consecutive elements.
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int l = threadIdx.x >> 5; l < nl; l += nw) {
       const long off = table.off[l];
       T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
-      for (int m = threadIdx.x; m < n; m += blockDim.x) {
-        if (off >= 0)
-          cp_async4(dst + 2 * m, a.data + off + m);
-        else
-          dst[2 * m] = T(0);
+      if (off >= 0) {
+        const T *src0 = a.data + off;
+        for (int m = lane; m < n; m += 32) cp_async4(dst + 2 * m, src0 + m);
+      } else {
+        for (int m = lane; m < n; m += 32) dst[2 * m] = T(0);
       }
     }
   }
@@ -602,18 +563,22 @@ __global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
     return comp ? (xm.x - xn.x) * h : (xn.y - xm.y) * h;
   };
   if (a.line_fast) {
-    const int cnt = nl * n;
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-      const int m = e >> a.lg_lines, l = e & (nl - 1);
-      const long off = table.off[l];
-      if (off >= 0) a.data[off + (long)m * a.se] = value(s + (l >> 1) * ROW, m, l & 1);
+    const int l = threadIdx.x & (nl - 1);
+    const long off = table.off[l];
+    if (off >= 0) {
+      const T2 *r = s + (l >> 1) * ROW;
+      T *dst0 = a.data + off;
+      const int ms = blockDim.x >> a.lg_lines;
+      for (int m = threadIdx.x >> a.lg_lines; m < n; m += ms) dst0[(long)m * a.se] = value(r, m, l & 1);
     }
   } else {
-    for (int l = 0; l < nl; ++l) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int l = threadIdx.x >> 5; l < nl; l += nw) {
       const long off = table.off[l];
       if (off < 0) continue;
       const T2 *r = s + (l >> 1) * ROW;
-      for (int m = threadIdx.x; m < n; m += blockDim.x) a.data[off + m] = value(r, m, l & 1);
+      T *dst0 = a.data + off;
+      for (int m = lane; m < n; m += 32) dst0[m] = value(r, m, l & 1);
     }
   }
 }
@@ -894,8 +859,7 @@ static LineArgs<T> make_args(const Geometry &g, const AxisPlan<T> &ax, int d, T 
 }
 
 template <typename T>
-int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark,
-                            T *const *vel, double dt) {
+int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, const std::function<void(int)> &mark) {
   const Geometry &g = geo;
   // Inverse normalisations, src/PressureEquation.cpp:167,200,234:
   // (points - 1) * (periodic ? 1 : 2), applied as a product with the reciprocal.
@@ -905,15 +869,6 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
     const AxisPlan<T> &ax = axis[d];
     LineArgs<T> a = make_args(g, ax, d, phi);
     a.scale = scale;
-    if (d == 0 && mode == kModeForward && vel) {
-      a.du = vel[0];
-      a.dv = vel[1];
-      a.dw = vel[2];
-      a.vsy = g.sy();
-      a.vsz = g.sz();
-      for (int q = 0; q < 3; ++q) a.doh[q] = T(g.oh[q]);
-      a.inv_dt = T(1.0 / dt);
-    }
     if (mode == kModeFwdEigInv) a.eig = eig;  // the z sweep's other axes are x (fast) and y
     const long total = (long)a.na * a.nb;
     if (ax.reg_n1) {
