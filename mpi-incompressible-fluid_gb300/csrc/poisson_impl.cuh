@@ -474,8 +474,15 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
   __syncthreads();
 }
 
+// Three CTAs per SM (at most 80 registers) where the transform fits without
+// meaningful spills; the fused z sweep of the 32-point shapes keeps two.
+template <int N1, int MODE>
+struct RegMinBlocks {
+  static constexpr int v = (MODE == 2 && N1 >= 32) ? 2 : 3;
+};
+
 template <typename T, int N1, int N2, int MODE, int KIND>
-__global__ void __launch_bounds__(kThreads, 2) line_kernel_reg(LineArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kernel_reg(LineArgs<T> a) {
   static_assert(sizeof(T) == 4, "the register path stages 4-byte elements");
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
