@@ -29,13 +29,14 @@ __device__ __forceinline__ T ld(const T *p, long q) {
 //
 // A stage adds an increment of O(dt) to an O(1) velocity; rounded to the
 // nearest float the increment loses a biased share of its bits every time,
-// and with dt ~ h^2 that error grows with the number of stages. The state
-// updates of the float path therefore round stochastically: the exact sum
-// s + e (TwoSum, Knuth) is rounded to the neighbour of s on e's side with
-// probability |e| / ulp, so the rounding errors have mean zero and add up as a
-// random walk. The draws come from a counter-based hash of the point, the
-// stage and the step's time (ten bits per update: a probability resolution of
-// 1/1024 ulp), so a run is deterministic.
+// and with dt ~ h^2 that error grows with the number of stages (increments
+// below half an ulp are lost entirely). The state updates of the float path
+// therefore round stochastically, in the dithered form: uniform noise in
+// [-1/2, 1/2) ulp of the state is added to the increment before the
+// round-to-nearest addition, so the rounded sum equals the exact one in
+// expectation and the rounding errors add up as a random walk. The draws come
+// from a counter-based hash of the point, the stage and the step's time (ten
+// bits per update), so a run is deterministic.
 __device__ __forceinline__ unsigned sr_mix(unsigned x) {
   // lowbias32 integer hash (public domain)
   x ^= x >> 16;
@@ -52,22 +53,17 @@ __device__ __forceinline__ unsigned sr_salt(const TimeRef &tr, unsigned tag) {
   return sr_mix((unsigned)b ^ (unsigned)(b >> 32) ^ (tag * 0x9e3779b9u));
 }
 
-// b + c rounded stochastically; r in [0, 1) is the draw. The neighbour of s on
-// e's side is one unit in the last place away from s: +1 in the bit pattern
-// when s and e have the same sign, -1 otherwise. Rounding to the neighbour
-// with probability |e| / ulp keeps the expected result b + c.
+// b + c with dither r in [-1/2, 1/2): ulp(b) from b's exponent bits (zero for
+// b = 0 and subnormals, where the addition is plain round-to-nearest).
 __device__ __forceinline__ float add_sr(float b, float c, float r) {
-  const float s = b + c;
-  const float bb = s - b;
-  const float e = (b - (s - bb)) + (c - bb);  // b + c == s + e exactly
-  const int sb = __float_as_int(s);
-  const float nb = __int_as_float(sb + (((sb ^ __float_as_int(e)) >> 31) | 1));
-  return (s != 0.f && fabsf(e) > r * fabsf(nb - s)) ? nb : s;
+  const int eb = (__float_as_int(b) & 0x7f800000) - (23 << 23);
+  const float ulp = __int_as_float(eb > 0 ? eb : 0);
+  return b + fmaf(r, ulp, c);
 }
 
-// Ten-bit uniform draw number `slot` (0..2) from a 32-bit hash.
+// Ten-bit dither number `slot` (0..2) from a 32-bit hash, in [-1/2, 1/2).
 __device__ __forceinline__ float sr_draw(unsigned h, int slot) {
-  return (float)((h >> (10 * slot)) & 1023u) * (1.0f / 1024.0f);
+  return (float)((h >> (10 * slot)) & 1023u) * (1.0f / 1024.0f) - 0.5f;
 }
 
 // state + increment: stochastically rounded in float (h: the draw), exact
@@ -283,16 +279,33 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
   // multiple of 8) and is copied as kHX / kVec vectors of 16 bytes; vectors
   // outside the box are zero-filled. Only the first kTX + 2 of a row are read.
   constexpr int kVec = 16 / sizeof(T), kVecRow = kHX / kVec, kVecPlane = kVecRow * kHY;
+  constexpr int kVecPer = (kVecPlane * 4 + kTX * kTY - 1) / (kTX * kTY);  // vectors per thread and plane
+  // This thread's tile vectors, fixed for every plane: shared-memory offset
+  // within a slot (-1: none), source pointer and in-plane offset (-1: outside
+  // the box, zero-filled).
+  int v_sm[kVecPer];
+  const T *v_src[kVecPer];
+  long v_off[kVecPer];
+#pragma unroll
+  for (int r = 0; r < kVecPer; ++r) {
+    const int e = threadIdx.x + r * kTX * kTY;
+    const int f = e / kVecPlane, ev = e - f * kVecPlane;
+    const int hy = ev / kVecRow, hx = (ev - hy * kVecRow) * kVec;
+    const int i = i0 - 1 + hx, j = j0 - 1 + hy;
+    v_sm[r] = f < nf ? (int)(&ring.f[f][0][hy * kHX + hx] - &ring.f[0][0][0]) : -1;
+    v_src[r] = f == 0 ? src[0] : (f == 1 ? src[1] : (f == 2 ? src[2] : src[3]));
+    v_off[r] = (i < g.PX && j < g.PY) ? (long)i + g.PX * (long)j : -1;
+  }
+  const long plane = g.sz();
+  T *const ring0 = &ring.f[0][0][0];
   auto load_plane = [&](int kk) {
     if (kk >= 0 && kk < g.PZ) {
-      for (int e = threadIdx.x; e < kVecPlane * nf; e += kTX * kTY) {
-        const int f = e / kVecPlane, ev = e - f * kVecPlane;
-        const int hy = ev / kVecRow, hx = (ev - hy * kVecRow) * kVec;
-        const int i = i0 - 1 + hx, j = j0 - 1 + hy;
-        T *d = &ring.f[f][kk & 3][hy * kHX + hx];
-        const T *sp = f == 0 ? src[0] : (f == 1 ? src[1] : (f == 2 ? src[2] : src[3]));
-        if (i < g.PX && j < g.PY)
-          cp_async16_st(d, sp + g.idx(i, j, kk));
+#pragma unroll
+      for (int r = 0; r < kVecPer; ++r) {
+        if (v_sm[r] < 0) continue;
+        T *d = ring0 + v_sm[r] + (kk & 3) * kPL;
+        if (v_off[r] >= 0)
+          cp_async16_st(d, v_src[r] + v_off[r] + kk * plane);
         else
           *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
       }
@@ -352,7 +365,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
         const T r1 = F.vel(2, c)[q];
         const T uu = F.vel(0, c)[q];
         F.vel(2, c)[q] = kSR ? state_add(uu, K.k1 * (K.k2 * r1), h) : uu + K.k1 * (K.k2 * r1);
-        F.vel(0, c)[q] = kSR ? state_add(uu, K.k1 * (K.k3 * r1 + K.k4 * r), 1.0f - h) : uu + K.k1 * (K.k3 * r1 + K.k4 * r);
+        F.vel(0, c)[q] = kSR ? state_add(uu, K.k1 * (K.k3 * r1 + K.k4 * r), -h) : uu + K.k1 * (K.k3 * r1 + K.k4 * r);
       } else {
         const T r1 = F.vel(2, c)[q];
         F.vel(1, c)[q] = kSR ? state_add(r1, K.k1 * (K.k2 * r), h) : r1 + K.k1 * (K.k2 * r);
