@@ -212,10 +212,12 @@ struct Ring {
 // Neighbour accessor on the ring: field f at (i + di, j + dj, k + dk).
 template <typename T>
 struct Tap {
-  const Ring<T> *r;
-  int k, base;  // base = (ty + 1) * kHX + tx + 1
+  // pl[dk + 1]: this thread's point in the slot of plane k + dk (field 0);
+  // field f is 4 slots further per field, so every read is a base pointer
+  // plus a compile-time offset.
+  const T *pl[3];
   __device__ __forceinline__ T operator()(int f, int di, int dj, int dk) const {
-    return r->f[f][(k + dk) & 3][base + dj * kHX + di];
+    return pl[dk + 1][f * 4 * kPL + dj * kHX + di];
   }
 };
 
@@ -317,7 +319,7 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
   load_plane(kbeg + 1);
   const int i = i0 + tx, j = j0 + ty;
   const long sy = g.sy(), sz = g.sz();
-  const Tap<T> base_tap{&ring, 0, (ty + 1) * kHX + tx + 1};
+  const T *const tap0 = &ring.f[0][0][(ty + 1) * kHX + tx + 1];
   typename ForcingEval<T>::Axis fx{}, fy{}, fz{};
   if (forcing) {
     fx = fe.axis(0, min(i, fe.maxE - 1));
@@ -328,8 +330,9 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
     if (forcing) fz = fe.axis(2, k);
     cp_wait1();
     __syncthreads();
-    Tap<T> A = base_tap;
-    A.k = k;
+    Tap<T> A;
+#pragma unroll
+    for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
     const long q = g.idx(i, j, k);
     const unsigned hq = std::is_same<T, float>::value ? sr_mix((unsigned)q ^ salt) : 0u;
 #pragma unroll
