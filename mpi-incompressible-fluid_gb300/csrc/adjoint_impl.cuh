@@ -44,24 +44,29 @@ __device__ __forceinline__ void cp_wait_adj() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
 
-__device__ __forceinline__ bool interior(const Geometry &g, int c, long i, long j, long k) {
+__device__ __forceinline__ bool interior(const Geometry &g, int c, int i, int j, int k) {
   return i >= 1 && j >= 1 && k >= 1 && i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
 }
 
-__device__ __forceinline__ bool owner(const Geometry &g, long i, long j, long k) {
+__device__ __forceinline__ bool owner(const Geometry &g, int i, int j, int k) {
   return i >= g.own_lo[0] && i < g.own_lo[0] + g.np[0] && j >= g.own_lo[1] && j < g.own_lo[1] + g.np[1] &&
          k >= g.own_lo[2] && k < g.own_lo[2] + g.np[2];
 }
 
 // Trapezoid weight of a pressure point: 1/2 per Neumann axis on which it is
-// an end point.
-__device__ __forceinline__ double trap_weight(const Geometry &g, long i, long j, long k) {
-  const long q[3] = {i, j, k};
-  double w = 1.0;
+// an end point; returned as the number of such axes (the weight is 2^-nb, a
+// power of two, so scaling by it or its inverse is exact in any precision).
+__device__ __forceinline__ int trap_halvings(const Geometry &g, int i, int j, int k) {
+  const int q[3] = {i, j, k};
+  int nb = 0;
 #pragma unroll
   for (int d = 0; d < 3; ++d)
-    if (!g.periodic[d] && (q[d] == 0 || q[d] == g.E[d] - 1)) w *= 0.5;
-  return w;
+    if (!g.periodic[d] && (q[d] == 0 || q[d] == g.E[d] - 1)) ++nb;
+  return nb;
+}
+template <typename T>
+__device__ __forceinline__ T trap_weight(const Geometry &g, int i, int j, int k) {
+  return T(1) / T(1 << trap_halvings(g, i, j, k));
 }
 
 // ---- transposed momentum right-hand side, shared-memory tiled ----
@@ -213,23 +218,23 @@ __global__ void __launch_bounds__(kATX *kATY) rhs_adjoint_tiled(Geometry g, Coef
 template <typename T>
 __global__ void grad_adjoint_kernel(Geometry g, T *out, const T *add, const T *m0, const T *m1, const T *m2,
                                     T scale, int weighted) {
-  const long i = blockIdx.x * blockDim.x + threadIdx.x;
-  const long j = blockIdx.y * blockDim.y + threadIdx.y;
-  const long k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
   if (i >= g.E[0] || j >= g.E[1]) return;
   const T *mu[3] = {m0, m1, m2};
+  const long q = g.idx(i, j, k);
+  const long st[3] = {1, g.sy(), g.sz()};
   T acc = T(0);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const long ei = c == 0, ej = c == 1, ek = c == 2;
-    T a = interior(g, c, i, j, k) ? mu[c][g.idx(i, j, k)] : T(0);
-    if (interior(g, c, i + ei, j + ej, k + ek)) a -= mu[c][g.idx(i + ei, j + ej, k + ek)];
+    T a = interior(g, c, i, j, k) ? mu[c][q] : T(0);
+    if (interior(g, c, i + (c == 0), j + (c == 1), k + (c == 2))) a -= mu[c][q + st[c]];
     acc += a * T(g.oh[c]);
   }
-  const long q = g.idx(i, j, k);
   T v = scale * acc;
   if (add) v += add[q];
-  if (weighted) v = T((double)v / trap_weight(g, i, j, k));
+  if (weighted) v *= T(1 << trap_halvings(g, i, j, k));
   out[q] = v;
 }
 
@@ -238,20 +243,19 @@ __global__ void grad_adjoint_kernel(Geometry g, T *out, const T *add, const T *m
 template <typename T>
 __global__ void div_adjoint_kernel(Geometry g, T *o0, T *o1, T *o2, const T *i0, const T *i1, const T *i2,
                                    const T *rho, T scale) {
-  const long i = blockIdx.x * blockDim.x + threadIdx.x;
-  const long j = blockIdx.y * blockDim.y + threadIdx.y;
-  const long k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
   T *out[3] = {o0, o1, o2};
   const T *in[3] = {i0, i1, i2};
-  const T r0 = owner(g, i, j, k) ? T((double)rho[g.idx(i, j, k)] * trap_weight(g, i, j, k)) : T(0);
+  const long q = g.idx(i, j, k);
+  const long st[3] = {1, g.sy(), g.sz()};
+  const T r0 = owner(g, i, j, k) ? rho[q] * trap_weight<T>(g, i, j, k) : T(0);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     if (i >= g.ext(c, 0) || j >= g.ext(c, 1) || k >= g.ext(c, 2)) continue;
-    const long ei = c == 0, ej = c == 1, ek = c == 2;
-    T rm = T(0);
-    if (owner(g, i - ei, j - ej, k - ek))
-      rm = T((double)rho[g.idx(i - ei, j - ej, k - ek)] * trap_weight(g, i - ei, j - ej, k - ek));
-    const long q = g.idx(i, j, k);
+    const int im = i - (c == 0), jm = j - (c == 1), km = k - (c == 2);
+    const T rm = owner(g, im, jm, km) ? rho[q - st[c]] * trap_weight<T>(g, im, jm, km) : T(0);
     out[c][q] = in[c][q] + scale * (rm - r0) * T(g.oh[c]);
   }
 }
@@ -305,11 +309,12 @@ __global__ void dirichlet_adjoint_kernel(Geometry g, T *f0, T *f1, T *f2) {
 
 // Sum of v over the block (32 x 8 threads) in a fixed order, written to
 // part[linear block index] by thread 0: deterministic partial sums.
-__device__ __forceinline__ void block_partial(double v, double *part) {
+template <typename A>
+__device__ __forceinline__ void block_partial(A v, double *part) {
   __shared__ double w[8];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  if ((t & 31) == 0) w[t >> 5] = v;
+  if ((t & 31) == 0) w[t >> 5] = (double)v;
   __syncthreads();
   if (t == 0) {
     double s = 0.0;
@@ -343,13 +348,13 @@ __global__ void sum_partials_kernel(const double *part, long n, double *out, int
 template <typename T>
 __global__ void split_kernel(Geometry g, T *m0, T *m1, T *m2, T *p0, T *p1, T *p2, const T *x0, const T *x1,
                              const T *x2, T a, T b, T a2, int write_pend, const T *tab, int maxE, double *part) {
-  const long i = blockIdx.x * blockDim.x + threadIdx.x;
-  const long j = blockIdx.y * blockDim.y + threadIdx.y;
-  const long k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
   T *mu[3] = {m0, m1, m2}, *pend[3] = {p0, p1, p2};
   const T *lx[3] = {x0, x1, x2};
   const long q = g.idx(i, j, k);
-  double f = 0.0;
+  T f = T(0);  // this point's share of mu . F (warp sums in T, block sums in double)
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     if (i >= g.ext(c, 0) || j >= g.ext(c, 1) || k >= g.ext(c, 2)) continue;
@@ -363,12 +368,12 @@ __global__ void split_kernel(Geometry g, T *m0, T *m1, T *m2, T *p0, T *p1, T *p
     mu[c][q] = m;
     if (write_pend) pend[c][q] = a2 * x;
     if (tab && c < 2) {
-      auto S = [&](int ax, int face, long n) { return (double)tab[((ax * 2 + face) * 2 + 0) * maxE + n]; };
-      auto C = [&](int ax, int face, long n) { return (double)tab[((ax * 2 + face) * 2 + 1) * maxE + n]; };
+      auto S = [&](int ax, int face, int n) { return tab[((ax * 2 + face) * 2 + 0) * maxE + n]; };
+      auto C = [&](int ax, int face, int n) { return tab[((ax * 2 + face) * 2 + 1) * maxE + n]; };
       if (c == 0)
-        f += (double)m * (S(0, 1, i) * C(1, 0, j) * C(2, 0, k));
+        f += m * (S(0, 1, i) * C(1, 0, j) * C(2, 0, k));
       else
-        f -= (double)m * (C(0, 0, i) * S(1, 1, j) * C(2, 0, k));
+        f -= m * (C(0, 0, i) * S(1, 1, j) * C(2, 0, k));
     }
   }
   if (tab) block_partial(f, part);
