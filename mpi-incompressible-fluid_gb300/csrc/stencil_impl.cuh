@@ -325,9 +325,34 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
     fx = fe.axis(0, min(i, fe.maxE - 1));
     fy = fe.axis(1, min(j, fe.maxE - 1));
   }
+  // Point values of the other sets the update reads at (i, j, k) (set 2 in
+  // Y3 and the velocity-only stages, set 0 in U* and the velocity-only Y3),
+  // prefetched into registers one plane ahead so their latency hides behind
+  // the stencil work.
+  constexpr bool kPre2 = ST == kStageY3 || ST == kVelY3 || ST == kVelUStar;
+  constexpr bool kPre0 = ST == kStageUStar || ST == kVelY3;
+  const bool in_box = i < g.PX && j < g.PY;
+  T n2[3] = {T(0), T(0), T(0)}, n0[3] = {T(0), T(0), T(0)};
+  auto prefetch = [&](int kk) {
+    if (!in_box || kk >= kend) return;
+    const long qq = g.idx(i, j, kk);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (kPre2) n2[c] = F.vel(2, c)[qq];
+      if (kPre0) n0[c] = F.vel(0, c)[qq];
+    }
+  };
+  prefetch(kbeg);
   for (int k = kbeg; k < kend; ++k) {
     load_plane(k + 2);
     if (forcing) fz = fe.axis(2, k);
+    T c2[3], c0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      c2[c] = n2[c];
+      c0[c] = n0[c];
+    }
+    prefetch(k + 1);
     cp_wait1();
     __syncthreads();
     Tap<T> A;
@@ -354,23 +379,23 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
         F.vel(1, c)[q] = kSR ? state_add(self, K.k1 * r - K.k3 * gp, h) : self + K.k1 * r - K.k3 * gp;
         F.vel(2, c)[q] = r;
       } else if (ST == kStageY3) {
-        const T r1 = F.vel(2, c)[q];
+        const T r1 = c2[c];
         const T r2s = K.k2 * r;
         F.vel(2, c)[q] = kSR ? state_add(self, K.k1 * r1 + r2s - K.k3 * gp, h) : self + K.k1 * r1 + r2s - K.k3 * gp;
         F.vel(0, c)[q] = r2s;
       } else if (ST == kStageUStar) {
-        const T r2s = -F.vel(0, c)[q];
+        const T r2s = -c0[c];
         F.vel(0, c)[q] = kSR ? state_add(self, r2s + K.k2 * r - K.k3 * gp, h) : self + r2s + K.k2 * r - K.k3 * gp;
       } else if (ST == kVelY2) {
         F.vel(2, c)[q] = r;
         F.vel(1, c)[q] = kSR ? state_add(self, K.k1 * r, h) : self + K.k1 * r;
       } else if (ST == kVelY3) {
-        const T r1 = F.vel(2, c)[q];
-        const T uu = F.vel(0, c)[q];
+        const T r1 = c2[c];
+        const T uu = c0[c];
         F.vel(2, c)[q] = kSR ? state_add(uu, K.k1 * (K.k2 * r1), h) : uu + K.k1 * (K.k2 * r1);
         F.vel(0, c)[q] = kSR ? state_add(uu, K.k1 * (K.k3 * r1 + K.k4 * r), -h) : uu + K.k1 * (K.k3 * r1 + K.k4 * r);
       } else {
-        const T r1 = F.vel(2, c)[q];
+        const T r1 = c2[c];
         F.vel(1, c)[q] = kSR ? state_add(r1, K.k1 * (K.k2 * r), h) : r1 + K.k1 * (K.k2 * r);
       }
     }
