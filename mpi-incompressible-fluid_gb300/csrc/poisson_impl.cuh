@@ -474,12 +474,12 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
   __syncthreads();
 }
 
-// Three CTAs per SM (at most 80 registers): the latency of the FFT's
-// dependent chains needs the warps more than the fused z sweep needs the
-// registers it spills.
+// Three CTAs per SM (at most 80 registers) where the transform fits without
+// meaningful spills; the fused z sweep of the 32-point shapes keeps two (at
+// three it spills ~150 bytes and ran 8% slower on GB300).
 template <int N1, int MODE>
 struct RegMinBlocks {
-  static constexpr int v = 3;
+  static constexpr int v = (MODE == 2 && N1 >= 32) ? 2 : 3;
 };
 
 template <typename T, int N1, int N2, int MODE, int KIND>
