@@ -419,12 +419,11 @@ __device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int
 #pragma unroll
   for (int c = 0; c < C; ++c) dd[c] = row[pad(c * N2 + t)];
   __syncthreads();
-  // E: X in natural order
+  // E: X in natural order, X_2k and X_2k+1 as one 16-byte store
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const int k = c * N2 + t;
-    row[2 * k] = ev[c];
-    row[2 * k + 1] = dd[c];
+    *reinterpret_cast<float4 *>(row + 2 * k) = make_float4(ev[c].x, ev[c].y, dd[c].x, dd[c].y);
   }
   if (t == N2 - 1) {
     T2 e;
@@ -580,13 +579,17 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
       for (int m = threadIdx.x >> a.lg_lines; m < n; m += ms) dst0[(long)m * a.se] = value(r, m, l & 1);
     }
   } else {
+    // one warp per line pair: each lane reads a complex element once and
+    // writes it to both lines
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int l = threadIdx.x >> 5; l < nl; l += nw) {
-      const long off = table.off[l];
-      if (off < 0) continue;
-      const T2 *r = s + (l >> 1) * ROW;
-      T *dst0 = a.data + off;
-      for (int m = lane; m < n; m += 32) dst0[m] = value(r, m, l & 1);
+    for (int p2 = threadIdx.x >> 5; p2 < nl / 2; p2 += nw) {
+      const long offa = table.off[2 * p2], offb = table.off[2 * p2 + 1];
+      const T2 *r = s + p2 * ROW;
+      T *da = a.data + offa, *db = a.data + offb;
+      for (int m = lane; m < n; m += 32) {
+        if (offa >= 0) da[m] = value(r, m, 0);
+        if (offb >= 0) db[m] = value(r, m, 1);
+      }
     }
   }
 }
@@ -713,7 +716,7 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
     reg_P = kThreads / reg_n2;
     reg_lg = 0;
     while ((1 << reg_lg) < 2 * reg_P) ++reg_lg;
-    reg_smem = sizeof(typename Vec2<T>::type) * (size_t)reg_P * (size_t)(reg_n1 * (reg_n2 + 1) + 1);
+    reg_smem = sizeof(typename Vec2<T>::type) * (size_t)reg_P * (size_t)(reg_n1 * (reg_n2 + 1) + 2);  // RegShape::ROW
   }
 
   // Twiddles exp(-2 pi i e / L) in long double, rounded once.

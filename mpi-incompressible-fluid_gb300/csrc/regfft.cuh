@@ -70,11 +70,12 @@ struct RegDft<T2, 2, SIGN> {
 };
 
 // Row stride (complex elements) for a pair: the N1 x (N2+1) padded transpose
-// plus one, so consecutive rows fall in different banks.
+// plus two, so consecutive rows fall in different banks and every row starts
+// 16-byte aligned (16-byte stores of two complex values).
 template <int N1, int N2>
 struct RegShape {
   static constexpr int L = N1 * N2;
-  static constexpr int ROW = N1 * (N2 + 1) + 1;
+  static constexpr int ROW = N1 * (N2 + 1) + 2;
 };
 
 }  // namespace mifgpu
