@@ -162,6 +162,23 @@ int mifgpu_adjust_pressure(mifgpu_ctx *ctx, double t);
  * (src/Norms.cpp:11-118). Reductions in double. */
 int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]);
 
+/* The reference's writers on velocity set 0 and the pressure
+ * (include/VTKDatExport.h:10-29, src/VTKDatExport.cpp), for one rank, with
+ * the reference's byte layouts; values are computed in the context's
+ * precision (double for MIFGPU_FP64, float for MIFGPU_MIXED, as the
+ * reference's Real), from the planes or lines fetched off the device:
+ *   write_vtk            planes x = 0, y = 0, z = 0, velocity interpolated
+ *                        to the pressure points and the pressure, binary
+ *                        big-endian unstructured-grid VTK (writeVTK); x = 0
+ *                        must lie in the domain (the reference asserts it)
+ *   write_dat            the profile line parallel to axis `direction`
+ *                        (0 x, 1 y, 2 z) through (x, y, z), which must lie on
+ *                        pressure planes or midway between them (writeDat)
+ *   write_vtk_full_mesh  every pressure point, ASCII VTK (writeVTKFullMesh) */
+int mifgpu_write_vtk(mifgpu_ctx *ctx, const char *filename);
+int mifgpu_write_dat(mifgpu_ctx *ctx, const char *filename, int direction, double x, double y, double z);
+int mifgpu_write_vtk_full_mesh(mifgpu_ctx *ctx, const char *filename);
+
 /* Kernel classes of one projection step, for mifgpu_profile_step. */
 enum mifgpu_prof_class {
   MIFGPU_PROF_STAGE = 0,      /* the three fused RK stage updates */

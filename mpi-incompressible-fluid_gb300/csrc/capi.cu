@@ -18,6 +18,7 @@
 #include "../../include/mifgpu.h"
 #include "adjoint_impl.cuh"
 #include "common.cuh"
+#include "export.cuh"
 #include "noalloc.cuh"
 #include "poisson.cuh"
 #include "stencil.cuh"
@@ -56,6 +57,7 @@ struct ImplBase {
   virtual int gradient(mifgpu_ctx *ctx, const GradRequest &req) = 0;
   virtual int download_adjoint(mifgpu_ctx *ctx, int id, double *host) = 0;
   virtual void drop_graphs() = 0;
+  virtual int fetch_box(mifgpu_ctx *ctx, int id, const int lo[3], const int n[3], double *out) = 0;
 };
 
 }  // namespace
@@ -146,6 +148,14 @@ void velocity_slot(double t_n, double dt, int kind, double Re, double *s) {
 }
 
 enum { kVariantProjection = 0, kVariantNhn = 1, kVariantVelocity = 2 };
+
+// Field values on an index box, converted to double, x fastest (the export writers' fetch).
+template <typename T>
+__global__ void box_gather_kernel(Geometry g, double *dst, const T *src, int lo0, int lo1, int lo2, int n0, int n1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= n0 || j >= n1) return;
+  dst[i + (long)n0 * (j + (long)n1 * k)] = (double)src[g.idx(lo0 + i, lo1 + j, lo2 + k)];
+}
 
 // Last node of every captured step: the next replay reads the next time slot.
 __global__ void advance_step_kernel(int *ctr) { *ctr += 1; }
@@ -767,6 +777,19 @@ struct Impl final : ImplBase {
     return MIFGPU_OK;
   }
 
+  int fetch_box(mifgpu_ctx *ctx, int id, const int lo[3], const int n[3], double *out) override {
+    if (int rc = ensure_staging(ctx)) return rc;
+    const T *src = id == kP ? F.f[kP] : F.vel(0, id);
+    const dim3 grid((unsigned)((n[0] + 31) / 32), (unsigned)((n[1] + 7) / 8), (unsigned)n[2]);
+    box_gather_kernel<T><<<grid, dim3(32, 8), 0, ctx->stream>>>(g, staging, src, lo[0], lo[1], lo[2], n[0], n[1]);
+    ++ctx->launches;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, staging, sizeof(double) * (size_t)n[0] * n[1] * n[2], cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MIFGPU_OK;
+  }
+
   // Captured graphs hold the stage scalars: drop them when one changes.
   void drop_graphs() override {
     drop_rev_graphs();
@@ -1055,6 +1078,44 @@ int mifgpu_velocity_error_norms_noalloc(mifgpu_ctx *ctx, double t, double out[3]
   out[1] = std::sqrt(h[1] * vol);
   out[2] = h[2];
   return MIFGPU_OK;
+}
+
+namespace {
+ExportSource export_source(mifgpu_ctx *ctx) {
+  ExportSource src;
+  src.g = ctx->g;
+  for (int d = 0; d < 3; ++d) src.size[d] = ctx->prm.size[d];
+  src.fp64 = ctx->prm.precision == MIFGPU_FP64;
+  src.fetch = [ctx](int id, const int lo[3], const int n[3], double *out) {
+    return ctx->impl->fetch_box(ctx, id, lo, n, out);
+  };
+  return src;
+}
+int export_result(mifgpu_ctx *ctx, int rc, const std::string &err) {
+  if (rc != MIFGPU_OK && !err.empty()) return fail(ctx, rc, err);
+  return rc;
+}
+}  // namespace
+
+int mifgpu_write_vtk(mifgpu_ctx *ctx, const char *filename) {
+  if (!ctx || !filename) return MIFGPU_EINVAL;
+  std::string err;
+  const int rc = export_vtk(export_source(ctx), filename, err);
+  return export_result(ctx, rc, err);
+}
+
+int mifgpu_write_dat(mifgpu_ctx *ctx, const char *filename, int direction, double x, double y, double z) {
+  if (!ctx || !filename) return MIFGPU_EINVAL;
+  std::string err;
+  const int rc = export_dat(export_source(ctx), filename, direction, x, y, z, err);
+  return export_result(ctx, rc, err);
+}
+
+int mifgpu_write_vtk_full_mesh(mifgpu_ctx *ctx, const char *filename) {
+  if (!ctx || !filename) return MIFGPU_EINVAL;
+  std::string err;
+  const int rc = export_vtk_full_mesh(export_source(ctx), filename, err);
+  return export_result(ctx, rc, err);
 }
 
 int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out) {

@@ -34,7 +34,8 @@ EXPORTED = [
     "mifgpu_timestep_velocity", "mifgpu_apply_bc", "mifgpu_solve_pressure", "mifgpu_divergence", "mifgpu_project",
     "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_profile_step", "mifgpu_launch_count",
     "mifgpu_device_bytes", "mifgpu_gradient_ke", "mifgpu_backward", "mifgpu_download_adjoint",
-    "mifgpu_set_forcing_amplitude", "mifgpu_velocity_error_norms_noalloc",
+    "mifgpu_set_forcing_amplitude", "mifgpu_velocity_error_norms_noalloc", "mifgpu_write_vtk",
+    "mifgpu_write_dat", "mifgpu_write_vtk_full_mesh",
 ]
 PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
                    "x_inverse", "periodic", "project"]
@@ -100,6 +101,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_download_adjoint": [vp, i, dp],
         "mifgpu_set_forcing_amplitude": [vp, d],
         "mifgpu_velocity_error_norms_noalloc": [vp, d, dp],
+        "mifgpu_write_vtk": [vp, C.c_char_p],
+        "mifgpu_write_dat": [vp, C.c_char_p, i, d, d, d],
+        "mifgpu_write_vtk_full_mesh": [vp, C.c_char_p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -253,6 +257,17 @@ class Solver:
         out = np.zeros(9)
         self._check(self.lib.mifgpu_error_norms(self.h, t, out.ctypes.data), "error_norms")
         return out
+
+    # -- the reference's writers (include/VTKDatExport.h) --
+    def write_vtk(self, filename: str) -> None:
+        self._check(self.lib.mifgpu_write_vtk(self.h, filename.encode()), "write_vtk")
+
+    def write_dat(self, filename: str, direction: int, x: float, y: float, z: float) -> None:
+        self._check(self.lib.mifgpu_write_dat(self.h, filename.encode(), int(direction), float(x), float(y), float(z)),
+                    "write_dat")
+
+    def write_vtk_full_mesh(self, filename: str) -> None:
+        self._check(self.lib.mifgpu_write_vtk_full_mesh(self.h, filename.encode()), "write_vtk_full_mesh")
 
     def velocity_error_norms_noalloc(self, t: float) -> np.ndarray:
         """L1, L2, Linf of the velocity error (error_norms()[0:3]) from a static

@@ -213,6 +213,23 @@ class RefSolver(_Solver):
     def available() -> bool:
         return os.path.exists(REF_LIB)
 
+    # The reference's exporters (include/VTKDatExport.h:10-29) on velocity
+    # set 0 and the pressure.
+    def write_vtk(self, filename: str) -> None:
+        fn = self._fn("write_vtk")
+        fn.argtypes = [C.c_void_p, C.c_char_p]
+        fn(self.h, filename.encode())
+
+    def write_dat(self, filename: str, direction: int, x: float, y: float, z: float) -> None:
+        fn = self._fn("write_dat")
+        fn.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_double, C.c_double, C.c_double]
+        fn(self.h, filename.encode(), int(direction), float(x), float(y), float(z))
+
+    def write_vtk_full_mesh(self, filename: str) -> None:
+        fn = self._fn("write_vtk_full_mesh")
+        fn.argtypes = [C.c_void_p, C.c_char_p]
+        fn(self.h, filename.encode())
+
 
 class OracleSolver(_Solver):
     """The plain-C restatement (oracle/libmif_oracle.so)."""

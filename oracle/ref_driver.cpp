@@ -10,7 +10,8 @@
  * 9 pressure; 10 pressure_buffer (the Poisson solution phi).
  * Call sites mirrored: test/full_test.cpp:60-175 (set-up, step loop, norms),
  * test/pressure_test_hn.cpp:40-70 (stand-alone Poisson solve),
- * test/velocity_test.cpp:75-90 (velocity-only step).
+ * test/velocity_test.cpp:75-90 (velocity-only step),
+ * src/main.cpp:162-172 and test/full_test.cpp:177-183 (VTK and DAT export).
  */
 #include <array>
 #include <cstring>
@@ -25,6 +26,7 @@
 #include "PressureTensor.h"
 #include "StaggeredTensorMacros.h"
 #include "Timestep.h"
+#include "VTKDatExport.h"
 #include "VelocityTensor.h"
 #include "manufactured.h"
 
@@ -235,6 +237,24 @@ int mifref_error_norms(void *h, double t, double out[9]) {
   out[6] = mif::ErrorL1Norm(pressure_gradient, *s->exact_pressure_gradient, t);
   out[7] = mif::ErrorL2Norm(pressure_gradient, *s->exact_pressure_gradient, t);
   out[8] = mif::ErrorLInfNorm(pressure_gradient, *s->exact_pressure_gradient, t);
+  return 0;
+}
+
+// The reference's exporters on velocity set 0 and the pressure
+// (include/VTKDatExport.h:10-29).
+int mifref_write_vtk(void *h, const char *filename) {
+  auto *s = static_cast<RefState *>(h);
+  mif::writeVTK(filename, *s->vel[0], *s->pressure);
+  return 0;
+}
+int mifref_write_dat(void *h, const char *filename, int direction, double x, double y, double z) {
+  auto *s = static_cast<RefState *>(h);
+  mif::writeDat(filename, *s->vel[0], *s->pressure, direction, x, y, z);
+  return 0;
+}
+int mifref_write_vtk_full_mesh(void *h, const char *filename) {
+  auto *s = static_cast<RefState *>(h);
+  mif::writeVTKFullMesh(filename, *s->vel[0], *s->pressure);
   return 0;
 }
 

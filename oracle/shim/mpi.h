@@ -12,7 +12,9 @@
  *   - Cartesian topology calls return the parent communicator and coordinate 0;
  *   - point-to-point calls are never reached with one rank (the reference
  *     guards them with prev/next_proc != -1, src/Constants.cpp:98-101), so
- *     they abort loudly if called.
+ *     they abort loudly if called;
+ *   - gathers copy the single contribution, MPI-IO writes go to a POSIX file
+ *     (src/VTKDatExport.cpp's writers).
  * A datatype handle encodes its extent in bytes, which is all a single rank
  * needs (MPI_Type_size, MPI_Type_contiguous).
  */
@@ -136,5 +138,47 @@ static inline int MPI_Allreduce(const void *sendbuf, void *recvbuf, int count, M
   return MPI_SUCCESS;
 }
 static inline int MPI_Bcast(void *, int, MPI_Datatype, int, MPI_Comm) { return MPI_SUCCESS; }
+
+/* Gathers: the single contribution is the whole result. */
+static inline int MPI_Allgather(const void *sendbuf, int scount, MPI_Datatype stype, void *recvbuf, int,
+                                MPI_Datatype, MPI_Comm) {
+  memmove(recvbuf, sendbuf, (size_t)scount * (size_t)stype);
+  return MPI_SUCCESS;
+}
+static inline int MPI_Gather(const void *sendbuf, int scount, MPI_Datatype stype, void *recvbuf, int,
+                             MPI_Datatype, int, MPI_Comm) {
+  memmove(recvbuf, sendbuf, (size_t)scount * (size_t)stype);
+  return MPI_SUCCESS;
+}
+/* The one contribution lands at the start of recvbuf. (writeDat computes its
+ * displacement array from element -1, src/VTKDatExport.cpp:529-531; with one
+ * rank the intended displacement is 0.) */
+static inline int MPI_Gatherv(const void *sendbuf, int scount, MPI_Datatype stype, void *recvbuf, const int *,
+                              const int *, MPI_Datatype, int, MPI_Comm) {
+  memmove(recvbuf, sendbuf, (size_t)scount * (size_t)stype);
+  return MPI_SUCCESS;
+}
+
+/* MPI-IO for one process: positioned writes on a POSIX file descriptor. An
+ * existing file is not truncated (the MPI standard's MPI_File_open). */
+#include <fcntl.h>
+#include <unistd.h>
+static inline int MPI_File_open(MPI_Comm, const char *filename, int amode, MPI_Info, MPI_File *fh) {
+  const int flags = ((amode & MPI_MODE_CREATE) ? O_CREAT : 0) | ((amode & MPI_MODE_WRONLY) ? O_WRONLY : O_RDONLY);
+  const int fd = open(filename, flags, 0644);
+  if (fd < 0) return 1;
+  *fh = fd;
+  return MPI_SUCCESS;
+}
+static inline int MPI_File_write_at(MPI_File fh, MPI_Offset offset, const void *buf, int count, MPI_Datatype t,
+                                    MPI_Status *) {
+  const size_t n = (size_t)count * (size_t)t;
+  return pwrite(fh, buf, n, (off_t)offset) == (ssize_t)n ? MPI_SUCCESS : 1;
+}
+static inline int MPI_File_close(MPI_File *fh) {
+  close(*fh);
+  *fh = -1;
+  return MPI_SUCCESS;
+}
 
 #endif /* ORACLE_SHIM_MPI_H */

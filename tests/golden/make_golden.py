@@ -61,8 +61,55 @@ def run_case(name, spec):
     print(f"{name}: {[a.shape for a in inputs.values()][:3]} ... norms {norms[:3]}")
 
 
+# The reference's writers (src/VTKDatExport.cpp) on the state after one step:
+# the state and the bytes of every file they write.
+EXPORT_CASES = {
+    "export_dirichlet": dict(case=dict(n_global=(9, 10, 11), size=(1.0, 1.0, 2.0), origin=(0.0, 0.0, -1.0),
+                                       Re=1000.0, dt=1e-4, exact_kind=O.KIND_ETHIER), init="exact",
+                             # (direction, x, y, z): y midway / z on planes; x on a plane; x midway (the y line
+                             # that reads v where u is meant)
+                             lines=[(0, 0.5, 0.5, 0.0), (1, 0.5, 0.5, 0.0), (2, 0.5, 0.5, 0.0), (1, 0.0625, 0.5, 0.0)]),
+    "export_channel": dict(case=dict(n_global=(9, 8, 10), size=(6.283185307179586, 2.0, 3.141592653589793),
+                                     origin=(0.0, -1.0, 0.0), Re=500.0, dt=1e-3, periodic=(True, False, True)),
+                           init="random", seed=5,
+                           lines=[(0, 0.0, 0.0, 0.0), (1, 0.0, 0.0, 0.0), (2, 0.0, 0.0, 0.0), (2, 0.3926990816987241, 0.0, 0.0)]),
+}
+
+
+def run_export_case(name, spec, tmpdir):
+    case = O.Case(**spec["case"])
+    ref = O.RefSolver(case)
+    if spec["init"] == "exact":
+        ref.set_exact_velocity(0, 0.0, True)
+        ref.set_exact_pressure(0.0)
+    else:
+        rng = np.random.default_rng(spec["seed"])
+        for n in ("u", "v", "w", "p"):
+            ref.set(n, rng.standard_normal(ref.shape(n)) * 0.1)
+    ref.timestep(0.0)
+    arrays = {f"state_{n}": ref.get(n) for n in ("u", "v", "w", "p")}
+    f = os.path.join(tmpdir, f"{name}.vtk")
+    ref.write_vtk(f)
+    arrays["vtk"] = np.frombuffer(open(f, "rb").read(), dtype=np.uint8)
+    f = os.path.join(tmpdir, f"{name}_full.vtk")
+    ref.write_vtk_full_mesh(f)
+    arrays["vtk_full"] = np.frombuffer(open(f, "rb").read(), dtype=np.uint8)
+    for q, (d, x, y, z) in enumerate(spec["lines"]):
+        f = os.path.join(tmpdir, f"{name}_{q}.dat")
+        ref.write_dat(f, d, x, y, z)
+        arrays[f"dat{q}"] = np.frombuffer(open(f, "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
+    print(f"{name}: vtk {arrays['vtk'].size} B, full {arrays['vtk_full'].size} B, "
+          f"dat {[arrays[f'dat{q}'].size for q in range(len(spec['lines']))]} B")
+
+
 if __name__ == "__main__":
+    import tempfile
+
     if not O.RefSolver.available():
         O.build()
     for name, spec in CASES.items():
         run_case(name, spec)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, spec in EXPORT_CASES.items():
+            run_export_case(name, spec, tmp)
