@@ -57,31 +57,83 @@ void pos_to_index(R pos, R mn, R delta, long &index, R &weight) {
   weight = R((float)imp);
 }
 
-// One field's values on a box of its indices; reads outside the box give 0
-// (they only occur multiplied by a zero weight).
-struct Box {
-  int lo[3] = {0, 0, 0}, n[3] = {0, 0, 0};
+// Values of one field on an index box (x fastest).
+struct Block {
+  long lo[3] = {0, 0, 0}, n[3] = {0, 0, 0};
   std::vector<double> v;
-  double at(long i, long j, long k) const {
+  bool get(long i, long j, long k, double &out) const {
     const long a = i - lo[0], b = j - lo[1], c = k - lo[2];
-    if (a < 0 || b < 0 || c < 0 || a >= n[0] || b >= n[1] || c >= n[2]) return 0.0;
-    return v[(size_t)(a + (long)n[0] * (b + (long)n[1] * c))];
+    if (a < 0 || b < 0 || c < 0 || a >= n[0] || b >= n[1] || c >= n[2]) return false;
+    out = v[(size_t)(a + n[0] * (b + n[1] * c))];
+    return true;
+  }
+};
+
+// One field on the index box the writers read. An index is resolved the way
+// the reference's tensors resolve it, through the flat offset
+// i + Ex (j + Ey k) of the field's storage (include/Tensor.h:137-140): on a
+// periodic x axis the writers read u one past the end of a row
+// (src/VTKDatExport.cpp:155, 391), which is the first element of the next
+// row, and likewise v one row past the end of a plane. `wrap` holds the
+// points such reads land on. Reads outside the storage give 0 (they only
+// occur multiplied by a zero weight, or past the last plane, where the
+// reference reads beyond its allocation).
+struct Box {
+  long ext[3] = {0, 0, 0};
+  Block main, wrap;
+  double at(long i, long j, long k) const {
+    const long f = i + ext[0] * (j + ext[1] * k);
+    if (f < 0 || f >= ext[0] * ext[1] * ext[2]) return 0.0;
+    const long fi = f % ext[0], fj = (f / ext[0]) % ext[1], fk = f / (ext[0] * ext[1]);
+    double x = 0.0;
+    if (main.get(fi, fj, fk, x) || wrap.get(fi, fj, fk, x)) return x;
+    return 0.0;
   }
 };
 
 // Extent of field id (0..2 velocity, 9 pressure) along axis d.
 int field_ext(const Geometry &g, int id, int d) { return id < 3 ? g.ext(id, d) : g.E[d]; }
 
-// Fetches field id on [lo, hi) clipped to its extents.
+int fetch_block(const ExportSource &src, int id, Block &blk) {
+  blk.v.assign((size_t)(blk.n[0] * blk.n[1] * blk.n[2]), 0.0);
+  if (blk.v.empty()) return MIFGPU_OK;
+  const int lo[3] = {(int)blk.lo[0], (int)blk.lo[1], (int)blk.lo[2]};
+  const int n[3] = {(int)blk.n[0], (int)blk.n[1], (int)blk.n[2]};
+  return src.fetch(id, lo, n, blk.v.data());
+}
+
+// Fetches field id for reads on [lo, hi): the box clipped to the field's
+// extents, and the bounding box of the in-storage points that reads past
+// the x or y extent resolve to.
 int fetch_box(const ExportSource &src, int id, const long lo[3], const long hi[3], Box &b) {
   for (int d = 0; d < 3; ++d) {
-    const long l = std::max(lo[d], 0L), h = std::min(hi[d], (long)field_ext(src.g, id, d));
-    b.lo[d] = (int)l;
-    b.n[d] = (int)std::max(h - l, 0L);
+    b.ext[d] = field_ext(src.g, id, d);
+    b.main.lo[d] = std::max(lo[d], 0L);
+    b.main.n[d] = std::max(std::min(hi[d], b.ext[d]) - b.main.lo[d], 0L);
   }
-  b.v.assign((size_t)b.n[0] * b.n[1] * b.n[2], 0.0);
-  if (b.v.empty()) return MIFGPU_OK;
-  return src.fetch(id, b.lo, b.n, b.v.data());
+  long wlo[3] = {b.ext[0], b.ext[1], b.ext[2]}, whi[3] = {0, 0, 0};
+  auto note = [&](long i, long j, long k) {
+    const long f = i + b.ext[0] * (j + b.ext[1] * k);
+    if (f < 0 || f >= b.ext[0] * b.ext[1] * b.ext[2]) return;
+    const long q[3] = {f % b.ext[0], (f / b.ext[0]) % b.ext[1], f / (b.ext[0] * b.ext[1])};
+    for (int d = 0; d < 3; ++d) {
+      wlo[d] = std::min(wlo[d], q[d]);
+      whi[d] = std::max(whi[d], q[d] + 1);
+    }
+  };
+  const long k0 = std::max(lo[2], 0L), j0 = std::max(lo[1], 0L);
+  for (long k = k0; k < hi[2]; ++k) {
+    for (long j = j0; j < hi[1]; ++j) {
+      const long i0 = j < b.ext[1] ? std::max(lo[0], b.ext[0]) : std::max(lo[0], 0L);
+      for (long i = i0; i < hi[0]; ++i) note(i, j, k);
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    b.wrap.lo[d] = wlo[d];
+    b.wrap.n[d] = std::max(whi[d] - wlo[d], 0L);
+  }
+  if (int rc = fetch_block(src, id, b.main)) return rc;
+  return fetch_block(src, id, b.wrap);
 }
 
 // The four fields on one index box (velocity set 0 and the pressure).

@@ -268,7 +268,7 @@ def test_autograd_function(mifgpu_lib, fp64_runs):
         m &= (x >= x0) & (x <= x1) & (y >= y0) & (y <= y1) & (z >= z0) & (z <= z1)
         loss = loss + 0.5 * vol * (o[torch.from_numpy(m)] ** 2).sum()
     loss.backward()
-    assert float(loss) == pytest.approx(r["loss"], rel=1e-12)
+    assert float(loss.detach()) == pytest.approx(r["loss"], rel=1e-12)
     for n, t in zip("uvwp", ins):
         np.testing.assert_allclose(t.grad.numpy(), g[n], rtol=0, atol=1e-13 * np.abs(g[n]).max())
     assert float(alpha.grad) == pytest.approx(r["dloss_dalpha"], rel=1e-12)
