@@ -334,56 +334,70 @@ __device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, 
 //   X_1 = sum_j d_j cos(pi j / N).
 // Two lines travel as z = a + i b; their Y_k are split from Z_k and Z_{N-k}.
 
-// Input element m < N of z for the pair, and the pair's partial X_1.
-template <typename T>
-__device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row, int m, int N,
-                                               const typename Vec2<T>::type *dsc, typename Vec2<T>::type &v,
+// Input element m = n1 N2 + t < N of z for the pair, and the pair's partial
+// X_1. (sin, cos)(pi m / N) comes from the thread's own angle pi t / N
+// (sct, from the table) and the compile-time angle pi n1 / N1 by the
+// angle-addition formulas.
+template <typename T, int N1>
+__device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row, int m, int n1, int N,
+                                               typename Vec2<T>::type sct, typename Vec2<T>::type &v,
                                                typename Vec2<T>::type &x1) {
   using T2 = typename Vec2<T>::type;
   const T2 xm = row[m], xn = row[N - m];
-  const T2 sc = __ldg(dsc + m);
+  const T cp = T(kCos64[n1 * (32 / N1)]), sp = T(kSin64[n1 * (32 / N1)]);
+  const T sn = sct.x * cp + sct.y * sp;  // sin(pi m / N)
+  const T cs = sct.y * cp - sct.x * sp;  // cos(pi m / N)
   const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
-  v.x = T(0.5) * sx - sc.x * dx;
-  v.y = T(0.5) * sy - sc.x * dy;
-  x1.x += sc.y * dx;
-  x1.y += sc.y * dy;
+  v.x = T(0.5) * sx - sn * dx;
+  v.y = T(0.5) * sy - sn * dy;
+  x1.x += cs * dx;
+  x1.y += cs * dy;
 }
 
-// row[k] = Z_k (k < N) of the pair -> row[m] = X_m (m <= N) of both lines.
-// The pair's N2 threads (consecutive lanes of one warp) own k = c N2 + t
-// (c < C = N / (2 N2)) for every bank-conflict-free pass over the row; the
-// running sum of the odd outputs is taken over contiguous blocks of C values
-// per thread, through a copy of D in the row at a padded index (k + k / C)
-// that makes those blocked accesses conflict-free too, and an exclusive scan
-// of the block totals across the lanes.
+// Z of the pair in registers (x[r*N2 + k2] = Z_k, k = t + N2 (r + R k2),
+// from reg_fft_core without STORE) -> row[m] = X_m (m <= N) of both lines.
+// Thread t takes k = c N2 + t for c < C = N1/2 (k < N/2); the mirror Z_{N-k}
+// is register c' = N1-1-c of lane N2-t (lane 0 keeps its own, c' = N1-c).
+// The running sum of the odd outputs is taken over contiguous blocks of C
+// values per thread, through a copy of D in the row at a padded index
+// (k + k / C) that makes the strided and blocked accesses bank-conflict
+// free, and an exclusive scan of the block totals across the lanes.
 template <typename T, int N1, int N2>
-__device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int t, typename Vec2<T>::type x1) {
+__device__ __forceinline__ void dct_half_output(const typename Vec2<T>::type (&x)[N1], typename Vec2<T>::type *row,
+                                                int t, typename Vec2<T>::type x1) {
   using T2 = typename Vec2<T>::type;
-  constexpr int N = N1 * N2, C = N1 / 2;
-  static_assert(N2 <= 32 && (N1 % 2) == 0, "pair within one warp");
+  constexpr int N = N1 * N2, C = N1 / 2, R = N1 / N2;
+  static_assert(N2 <= 32 && (N1 % 2) == 0 && R >= 1, "pair within one warp");
   auto pad = [](int k) { return k + k / C; };
+  auto reg = [](int c) { return (c % R) * N2 + c / R; };  // register of Z_{c N2 + t}
 #pragma unroll
   for (int o = N2 / 2; o > 0; o >>= 1) {
     x1.x += __shfl_xor_sync(0xffffffffu, x1.x, o, N2);
     x1.y += __shfl_xor_sync(0xffffffffu, x1.y, o, N2);
   }
-  // A: even outputs and the odd-output increments D_k (D_0 = 0), strided
+  const int partner = (N2 - t) & (N2 - 1);
+  const T2 zh = x[reg(C)];  // Z_{N/2} on lane 0
+  // A: even outputs, kept, and the odd-output increments D_k (D_0 = 0),
+  // straight to the padded scratch (the row is free: reg_fft_core ended with
+  // a warp barrier after its last read)
   T2 ev[C], dd[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int k = c * N2 + t;
-    const T2 zk = row[k], zn = row[(N - k) & (N - 1)];
+    const T2 zk = x[reg(c)];
+    const T2 send = x[reg(N1 - 1 - c)];
+    T2 zn;
+    zn.x = __shfl_sync(0xffffffffu, send.x, partner, N2);
+    zn.y = __shfl_sync(0xffffffffu, send.y, partner, N2);
+    if (t == 0) zn = c == 0 ? zk : x[reg(N1 - c)];
     ev[c].x = zk.x + zn.x;
     ev[c].y = zk.y + zn.y;
-    dd[c].x = k ? zn.y - zk.y : T(0);
-    dd[c].y = k ? zk.x - zn.x : T(0);
+    const bool k0 = c == 0 && t == 0;
+    T2 d;
+    d.x = k0 ? T(0) : zn.y - zk.y;
+    d.y = k0 ? T(0) : zk.x - zn.x;
+    row[pad(c * N2 + t)] = d;
   }
-  const T2 zh = row[N / 2];
-  __syncthreads();
-  // B: D to the padded scratch (the row is free now)
-#pragma unroll
-  for (int c = 0; c < C; ++c) row[pad(c * N2 + t)] = dd[c];
-  __syncthreads();
+  __syncwarp();
   // C: blocked running sums, then the block offsets across the lanes
   T2 run = {T(0), T(0)};
 #pragma unroll
@@ -407,6 +421,7 @@ __device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int
   excl.x = __shfl_up_sync(0xffffffffu, incl.x, 1, N2);
   excl.y = __shfl_up_sync(0xffffffffu, incl.y, 1, N2);
   if (t == 0) excl.x = excl.y = T(0);
+  __syncwarp();
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     T2 o;
@@ -414,44 +429,56 @@ __device__ __forceinline__ void dct_half_output(typename Vec2<T>::type *row, int
     o.y = x1.y + (excl.y + dd[c].y);
     row[pad(t * C + c)] = o;
   }
-  __syncthreads();
+  __syncwarp();
   // D: the odd outputs back in the strided order
 #pragma unroll
   for (int c = 0; c < C; ++c) dd[c] = row[pad(c * N2 + t)];
-  __syncthreads();
+  __syncwarp();
   // E: X in natural order, X_2k and X_2k+1 as one 16-byte store
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const int k = c * N2 + t;
     *reinterpret_cast<float4 *>(row + 2 * k) = make_float4(ev[c].x, ev[c].y, dd[c].x, dd[c].y);
   }
-  if (t == N2 - 1) {
+  if (t == 0) {
     T2 e;
     e.x = T(2) * zh.x;
     e.y = T(2) * zh.y;
     row[N] = e;
   }
-  __syncthreads();
+  __syncwarp();
+}
+
+// Twiddles W_L^(t k1), k1 = 1..N1-1, for thread t of a pair, one table
+// read each. (Forming them as products W^(4ta) W^(tb) of fewer reads raised
+// the 80-register kernels' spills, the loads being hoisted together.)
+template <typename T, int N1, int L>
+__device__ __forceinline__ void reg_twiddle_mul(typename Vec2<T>::type (&x)[N1], int t,
+                                                const typename Vec2<T>::type *tw) {
+#pragma unroll
+  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], __ldg(tw + ((t * k1) & (L - 1))));
 }
 
 // One length-L forward FFT (exponent sign -1) of the pair owned by this
 // thread group, in two register passes; x holds the thread's inputs
-// x[n1] = z[n1*N2 + t] and the result X[k] lands in row[k], conjugated when
-// conj_out is set. (A sign +1 transform is conj(FFT(conj(z))): callers
-// conjugate the input and set conj_out, so only one copy of this code exists
-// per kernel.)
-template <typename T, int N1, int N2>
+// x[n1] = z[n1*N2 + t]. With STORE the result X[k] lands in row[k],
+// conjugated when conj_out is set (a sign +1 transform is
+// conj(FFT(conj(z))): callers conjugate the input and set conj_out, so only
+// one copy of this code exists per kernel); without STORE it stays in
+// registers, x[r*N2 + k2] = X[t + r*N2 + N1*k2]. Every access is to the
+// pair's own row, and a pair's N2 threads are lanes of one warp, so the
+// phases are ordered by warp barriers.
+template <typename T, int N1, int N2, bool STORE = true>
 __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], typename Vec2<T>::type *row, int t,
                                              const typename Vec2<T>::type *tw, bool conj_out) {
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
   RegDft<T2, N1, -1>::run(x);
-#pragma unroll
-  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], tw[(t * k1) & (L - 1)]);
-  __syncthreads();  // every thread has read its inputs from the row
+  reg_twiddle_mul<T, N1, L>(x, t, tw);
+  __syncwarp();  // every thread of the pair has read its inputs from the row
 #pragma unroll
   for (int k1 = 0; k1 < N1; ++k1) row[k1 * (N2 + 1) + t] = x[k1];
-  __syncthreads();
+  __syncwarp();
   constexpr int R = N1 / N2;  // columns per thread
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -460,17 +487,19 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
     for (int n2 = 0; n2 < N2; ++n2) x[r * N2 + n2] = row[k1 * (N2 + 1) + n2];
     RegDft<T2, N2, -1>::run(x + r * N2);
   }
-  __syncthreads();
-  const T sy = conj_out ? T(-1) : T(1);
+  __syncwarp();
+  if constexpr (STORE) {
+    const T sy = conj_out ? T(-1) : T(1);
 #pragma unroll
-  for (int r = 0; r < R; ++r)
+    for (int r = 0; r < R; ++r)
 #pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) {
-      T2 v = x[r * N2 + k2];
-      v.y *= sy;
-      row[t + r * N2 + N1 * k2] = v;
-    }
-  __syncthreads();
+      for (int k2 = 0; k2 < N2; ++k2) {
+        T2 v = x[r * N2 + k2];
+        v.y *= sy;
+        row[t + r * N2 + N1 * k2] = v;
+      }
+    __syncwarp();
+  }
 }
 
 // Three CTAs per SM (at most 80 registers) where the transform fits without
@@ -538,16 +567,18 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
     const bool plus = KIND == 1 && (MODE == kModeInverse || pass == 1);
     if (pass == 1) {
       reg_eig_row<T, L, KIND == 2 ? 0 : KIND>(row, t, N2, n, ea, eb);
-      __syncthreads();
+      __syncwarp();
     }
     T2 x[N1];
     T2 x1 = {T(0), T(0)};  // kind 2: the pair's partial X_1
+    T2 sct = {T(0), T(1)};
+    if (KIND == 2) sct = __ldg(a.dsc + t);
 #pragma unroll
     for (int n1 = 0; n1 < N1; ++n1) {
       const int m = n1 * N2 + t;
       T2 v;
       if (KIND == 2) {
-        dct_half_input<T>(row, m, L, a.dsc, v, x1);
+        dct_half_input<T, N1>(row, m, n1, L, sct, v, x1);
       } else {
         v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
                       : row[KIND == 0 ? (m < n ? m : L - m) : m];
@@ -555,9 +586,14 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
       if (plus) v.y = -v.y;
       x[n1] = v;
     }
-    reg_fft_core<T, N1, N2>(x, row, t, a.tw, plus);
-    if (KIND == 2) dct_half_output<T, N1, N2>(row, t, x1);
+    if constexpr (KIND == 2) {
+      reg_fft_core<T, N1, N2, false>(x, row, t, a.tw, false);
+      dct_half_output<T, N1, N2>(x, row, t, x1);
+    } else {
+      reg_fft_core<T, N1, N2>(x, row, t, a.tw, plus);
+    }
   }
+  __syncthreads();  // the stores below read other pairs' rows
   // store: row[m] holds X[m]; the forward real DFT splits the pair into
   // FFTW's half-complex order on the way out.
   const T scale = T(a.scale);
