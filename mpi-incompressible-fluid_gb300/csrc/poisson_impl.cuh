@@ -69,7 +69,7 @@ struct LineArgs {
   int line_fast;          // 1: consecutive threads take consecutive lines (strided axes)
   double scale;           // output multiplier (inverse normalisation), 1 otherwise
   // kModeFwdEigInv only: 1/(lambda_x + lambda_y + lambda_z) on the owner block,
-  // x fastest, computed in double at set-up, zero mode 0.
+  // z fastest, computed in double at set-up, zero mode 0.
   const T *eig;
 };
 
@@ -271,11 +271,10 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
 
-// Element m of the first FFT's input: the even extension (DCT-I), the plain
+// Element m of the first FFT's input for a real-DFT line pair: the plain
 // pair (R2HC), or Z_k = A_k + i B_k rebuilt from two half-complex lines (HC2R).
 template <typename T2, typename Src>
-__device__ __forceinline__ T2 reg_input(const Src &src, int m, int n, int L, int kind, bool hc2r) {
-  if (kind == 0) return src(m < n ? m : L - m);
+__device__ __forceinline__ T2 reg_input(const Src &src, int m, int L, bool hc2r) {
   if (!hc2r || m == 0 || 2 * m == L) return src(m);
   T2 z;
   if (2 * m < L) {
@@ -290,23 +289,16 @@ __device__ __forceinline__ T2 reg_input(const Src &src, int m, int n, int L, int
   return z;
 }
 
-// The z sweep's eigenvalue product on the spectrum X of the pair (natural
-// order in row), in place, by the N2 threads of the pair: DCT-I scales each
-// line's real spectrum; the real DFT forms eig_a A_m + i eig_b B_m with
-// A = (X_m + conj X_-m)/2, B = (X_m - conj X_-m)/(2i), pairwise for (m, L-m).
-template <typename T, int L, int KIND>
-__device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, int stride, int n, const T *ea,
+// The z sweep's eigenvalue product for a periodic z axis, on the spectrum X
+// of the pair (natural order in row), in place, by the N2 threads of the
+// pair: eig_a A_m + i eig_b B_m with A = (X_m + conj X_-m)/2,
+// B = (X_m - conj X_-m)/(2i), pairwise for (m, L-m), ea and eb the lines'
+// rows of the 1/lambda table. (DCT-I lines are scaled by dct_half_output as
+// it stores their spectra.)
+template <typename T, int L>
+__device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, int stride, const T *ea,
                                             const T *eb) {
   using T2 = typename Vec2<T>::type;
-  if (KIND == 0) {
-    for (int m = t; m < n; m += stride) {
-      T2 v = row[m];
-      v.x = v.x * __ldg(ea + m);
-      v.y = v.y * __ldg(eb + m);
-      row[m] = v;
-    }
-    return;
-  }
   const T h = T(0.5);
   for (int m = t; 2 * m <= L; m += stride) {
     const int mn = (L - m) & (L - 1);
@@ -364,7 +356,8 @@ __device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row
 // free, and an exclusive scan of the block totals across the lanes.
 template <typename T, int N1, int N2>
 __device__ __forceinline__ void dct_half_output(const typename Vec2<T>::type (&x)[N1], typename Vec2<T>::type *row,
-                                                int t, typename Vec2<T>::type x1) {
+                                                int t, typename Vec2<T>::type x1, const T *ea,
+                                                const T *eb) {
   using T2 = typename Vec2<T>::type;
   constexpr int N = N1 * N2, C = N1 / 2, R = N1 / N2;
   static_assert(N2 <= 32 && (N1 % 2) == 0 && R >= 1, "pair within one warp");
@@ -434,16 +427,28 @@ __device__ __forceinline__ void dct_half_output(const typename Vec2<T>::type (&x
 #pragma unroll
   for (int c = 0; c < C; ++c) dd[c] = row[pad(c * N2 + t)];
   __syncwarp();
-  // E: X in natural order, X_2k and X_2k+1 as one 16-byte store
+  // E: X in natural order, X_2k and X_2k+1 as one 16-byte store; with the
+  // 1/lambda rows ea, eb (the z sweep's first pass) scaled on the way
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const int k = c * N2 + t;
-    *reinterpret_cast<float4 *>(row + 2 * k) = make_float4(ev[c].x, ev[c].y, dd[c].x, dd[c].y);
+    float4 o = make_float4(ev[c].x, ev[c].y, dd[c].x, dd[c].y);
+    if (ea) {
+      o.x *= __ldg(ea + 2 * k);
+      o.y *= __ldg(eb + 2 * k);
+      o.z *= __ldg(ea + 2 * k + 1);
+      o.w *= __ldg(eb + 2 * k + 1);
+    }
+    *reinterpret_cast<float4 *>(row + 2 * k) = o;
   }
   if (t == 0) {
     T2 e;
     e.x = T(2) * zh.x;
     e.y = T(2) * zh.y;
+    if (ea) {
+      e.x *= __ldg(ea + N);
+      e.y *= __ldg(eb + N);
+    }
     row[N] = e;
   }
   __syncwarp();
@@ -513,6 +518,7 @@ struct RegMinBlocks {
 template <typename T, int N1, int N2, int MODE, int KIND>
 __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kernel_reg(LineArgs<T> a) {
   static_assert(sizeof(T) == 4, "the register path stages 4-byte elements");
+  static_assert(KIND == 1 || KIND == 2, "real DFT or half-length DCT-I");
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
   constexpr int ROW = RegShape<N1, N2>::ROW;
@@ -527,9 +533,12 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   const int nl = 2 * a.P;
 
   fill_line_table(table, a, line0, total);
+  // One 128-byte global segment per warp access: strided lines put 32
+  // consecutive lines (consecutive addresses) on the lanes of a warp at one m,
+  // x lines put a warp on one line. (Splitting a warp into two 16-line or
+  // two-line halves makes the 4-byte shared-memory writes conflict free but
+  // halves the segments, and ran slower.)
   if (a.line_fast) {
-    // Strided lines: consecutive threads own consecutive lines (consecutive
-    // addresses at each m); each thread keeps its line and walks m.
     const int l = threadIdx.x & (nl - 1);
     const long off = table.off[l];
     T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
@@ -541,7 +550,6 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
       for (int m = threadIdx.x >> a.lg_lines; m < n; m += ms) dst[2 * m] = T(0);
     }
   } else {
-    // Contiguous x lines: one warp per line, lanes on consecutive elements.
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int l = threadIdx.x >> 5; l < nl; l += nw) {
       const long off = table.off[l];
@@ -553,6 +561,17 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
         for (int m = lane; m < n; m += 32) dst[2 * m] = T(0);
       }
     }
+  }
+  if (MODE == kModeFwdEigInv) {
+    // The CTA's 1/lambda rows (consecutive lines, z fastest: one contiguous
+    // range) towards L2 while the lines load; the first pass reads them when
+    // it stores its spectra.
+    const long last = min(line0 + nl, total) - 1;
+    const char *e0 = reinterpret_cast<const char *>(a.eig + table.eoff[0] * n);
+    const char *e1 = reinterpret_cast<const char *>(a.eig + (table.eoff[last - line0] + 1) * n);
+    if (table.eoff[last - line0] == table.eoff[0] + (last - line0))
+      for (const char *q = e0 + 128 * threadIdx.x; q < e1; q += 128 * kThreads)
+        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(q));
   }
   cp_async_wait_all();
   __syncthreads();
@@ -566,8 +585,10 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
     // product and the inverse transform of the z sweep
     const bool plus = KIND == 1 && (MODE == kModeInverse || pass == 1);
     if (pass == 1) {
-      reg_eig_row<T, L, KIND == 2 ? 0 : KIND>(row, t, N2, n, ea, eb);
-      __syncwarp();
+      if (KIND != 2) {
+        reg_eig_row<T, L>(row, t, N2, ea, eb);
+        __syncwarp();
+      }
     }
     T2 x[N1];
     T2 x1 = {T(0), T(0)};  // kind 2: the pair's partial X_1
@@ -580,15 +601,16 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
       if (KIND == 2) {
         dct_half_input<T, N1>(row, m, n1, L, sct, v, x1);
       } else {
-        v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, n, L, KIND, MODE == kModeInverse && KIND == 1)
-                      : row[KIND == 0 ? (m < n ? m : L - m) : m];
+        v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, L, MODE == kModeInverse)
+                      : row[m];
       }
       if (plus) v.y = -v.y;
       x[n1] = v;
     }
     if constexpr (KIND == 2) {
       reg_fft_core<T, N1, N2, false>(x, row, t, a.tw, false);
-      dct_half_output<T, N1, N2>(x, row, t, x1);
+      const bool scale_eig = MODE == kModeFwdEigInv && pass == 0;
+      dct_half_output<T, N1, N2>(x, row, t, x1, scale_eig ? ea : nullptr, scale_eig ? eb : nullptr);
     } else {
       reg_fft_core<T, N1, N2>(x, row, t, a.tw, plus);
     }
@@ -650,10 +672,7 @@ const void *reg_kernel_ptr(int mode, int kind) {
     return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 2>
            : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 2>
                                   : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 2>;
-  if (kind == 0)
-    return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 0>
-           : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 0>
-                                  : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 0>;
+  if (kind != 1) return nullptr;  // a DCT-I axis always takes the half-length form (kind 2) here
   return mode == kModeForward   ? (const void *)line_kernel_reg<T, A, B, kModeForward, 1>
          : mode == kModeInverse ? (const void *)line_kernel_reg<T, A, B, kModeInverse, 1>
                                 : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 1>;
