@@ -221,44 +221,59 @@ struct Tap {
   }
 };
 
-// include/MomentumEquation.h:42-255 (OPT_CPU_CACHE branch) on the ring.
+// Every ring value the three momentum components and the pressure gradient
+// read at one point (31 distinct taps), named by the reference's stencil
+// numbering (include/MomentumEquation.h: 14 the point, 13/15 x-1/x+1,
+// 11/17 y-1/y+1, 5/23 z-1/z+1, and the mixed corners). They are read once,
+// before any store: the stores go to global memory through generic pointers,
+// which the compiler cannot separate from the ring, so reads interleaved
+// with them would be repeated per component.
 template <typename T>
-__device__ __forceinline__ T rhs_tap(int c, const Tap<T> &A, const Coeffs<T> &co) {
+struct Taps {
+  T u5, u6, u11, u12, u13, u14, u15, u17, u23;
+  T v5, v8, v11, v13, v14, v15, v16, v17, v23;
+  T w5, w11, w13, w14, w15, w17, w20, w22, w23;
+  T p5, p11, p13, p14;
+  __device__ __forceinline__ void load(const Tap<T> &A, bool with_p) {
+    u13 = A(0, -1, 0, 0), u11 = A(0, 0, -1, 0), u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u23 = A(0, 0, 0, 1);
+    u17 = A(0, 0, 1, 0), u15 = A(0, 1, 0, 0), u12 = A(0, 1, -1, 0), u6 = A(0, 1, 0, -1);
+    v13 = A(1, -1, 0, 0), v16 = A(1, -1, 1, 0), v14 = A(1, 0, 0, 0), v17 = A(1, 0, 1, 0), v11 = A(1, 0, -1, 0);
+    v5 = A(1, 0, 0, -1), v23 = A(1, 0, 0, 1), v15 = A(1, 1, 0, 0), v8 = A(1, 0, 1, -1);
+    w13 = A(2, -1, 0, 0), w22 = A(2, -1, 0, 1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1), w11 = A(2, 0, -1, 0);
+    w20 = A(2, 0, -1, 1), w5 = A(2, 0, 0, -1), w17 = A(2, 0, 1, 0), w15 = A(2, 1, 0, 0);
+    if (with_p) p14 = A(3, 0, 0, 0), p13 = A(3, -1, 0, 0), p11 = A(3, 0, -1, 0), p5 = A(3, 0, 0, -1);
+  }
+  __device__ __forceinline__ T self(int c) const { return c == 0 ? u14 : (c == 1 ? v14 : w14); }
+  // p at the point minus p one step back along axis c
+  __device__ __forceinline__ T dp(int c) const { return p14 - (c == 0 ? p13 : (c == 1 ? p11 : p5)); }
+};
+
+// include/MomentumEquation.h:42-255 (OPT_CPU_CACHE branch), term for term.
+template <typename T>
+__device__ __forceinline__ T rhs_taps(int c, const Taps<T> &a, const Coeffs<T> &co) {
   if (c == 0) {
-    const T u13 = A(0, -1, 0, 0), u11 = A(0, 0, -1, 0), u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u23 = A(0, 0, 0, 1),
-            u17 = A(0, 0, 1, 0), u15 = A(0, 1, 0, 0);
-    const T v13 = A(1, -1, 0, 0), v16 = A(1, -1, 1, 0), v14 = A(1, 0, 0, 0), v17 = A(1, 0, 1, 0);
-    const T w13 = A(2, -1, 0, 0), w22 = A(2, -1, 0, 1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1);
-    const T conv = -u14 * (u15 - u13) * co.o2h[0] - (v17 + v14 + v16 + v13) * (u17 - u11) * co.o8h[1] -
-                   (w23 + w14 + w22 + w13) * (u23 - u5) * co.o8h[2];
-    const T diff = (u15 - T(2) * u14 + u13) * co.oh2Re[0] + (u17 - T(2) * u14 + u11) * co.oh2Re[1] +
-                   (u23 - T(2) * u14 + u5) * co.oh2Re[2];
+    const T conv = -a.u14 * (a.u15 - a.u13) * co.o2h[0] - (a.v17 + a.v14 + a.v16 + a.v13) * (a.u17 - a.u11) * co.o8h[1] -
+                   (a.w23 + a.w14 + a.w22 + a.w13) * (a.u23 - a.u5) * co.o8h[2];
+    const T diff = (a.u15 - T(2) * a.u14 + a.u13) * co.oh2Re[0] + (a.u17 - T(2) * a.u14 + a.u11) * co.oh2Re[1] +
+                   (a.u23 - T(2) * a.u14 + a.u5) * co.oh2Re[2];
     return conv + diff;
   }
   if (c == 1) {
-    const T u11 = A(0, 0, -1, 0), u14 = A(0, 0, 0, 0), u12 = A(0, 1, -1, 0), u15 = A(0, 1, 0, 0);
-    const T v13 = A(1, -1, 0, 0), v11 = A(1, 0, -1, 0), v5 = A(1, 0, 0, -1), v14 = A(1, 0, 0, 0), v23 = A(1, 0, 0, 1),
-            v17 = A(1, 0, 1, 0), v15 = A(1, 1, 0, 0);
-    const T w11 = A(2, 0, -1, 0), w20 = A(2, 0, -1, 1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1);
-    const T conv = -(u15 + u14 + u12 + u11) * (v15 - v13) * co.o8h[0] - v14 * (v17 - v11) * co.o2h[1] -
-                   (w23 + w14 + w20 + w11) * (v23 - v5) * co.o8h[2];
-    const T diff = (v15 - T(2) * v14 + v13) * co.oh2Re[0] + (v17 - T(2) * v14 + v11) * co.oh2Re[1] +
-                   (v23 - T(2) * v14 + v5) * co.oh2Re[2];
+    const T conv = -(a.u15 + a.u14 + a.u12 + a.u11) * (a.v15 - a.v13) * co.o8h[0] - a.v14 * (a.v17 - a.v11) * co.o2h[1] -
+                   (a.w23 + a.w14 + a.w20 + a.w11) * (a.v23 - a.v5) * co.o8h[2];
+    const T diff = (a.v15 - T(2) * a.v14 + a.v13) * co.oh2Re[0] + (a.v17 - T(2) * a.v14 + a.v11) * co.oh2Re[1] +
+                   (a.v23 - T(2) * a.v14 + a.v5) * co.oh2Re[2];
     return conv + diff;
   }
-  const T u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u6 = A(0, 1, 0, -1), u15 = A(0, 1, 0, 0);
-  const T v5 = A(1, 0, 0, -1), v14 = A(1, 0, 0, 0), v8 = A(1, 0, 1, -1), v17 = A(1, 0, 1, 0);
-  const T w13 = A(2, -1, 0, 0), w11 = A(2, 0, -1, 0), w5 = A(2, 0, 0, -1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1),
-          w17 = A(2, 0, 1, 0), w15 = A(2, 1, 0, 0);
-  const T conv = -(u15 + u14 + u6 + u5) * (w15 - w13) * co.o8h[0] - (v17 + v14 + v8 + v5) * (w17 - w11) * co.o8h[1] -
-                 w14 * (w23 - w5) * co.o2h[2];
-  const T diff = (w15 - T(2) * w14 + w13) * co.oh2Re[0] + (w17 - T(2) * w14 + w11) * co.oh2Re[1] +
-                 (w23 - T(2) * w14 + w5) * co.oh2Re[2];
+  const T conv = -(a.u15 + a.u14 + a.u6 + a.u5) * (a.w15 - a.w13) * co.o8h[0] -
+                 (a.v17 + a.v14 + a.v8 + a.v5) * (a.w17 - a.w11) * co.o8h[1] - a.w14 * (a.w23 - a.w5) * co.o2h[2];
+  const T diff = (a.w15 - T(2) * a.w14 + a.w13) * co.oh2Re[0] + (a.w17 - T(2) * a.w14 + a.w11) * co.oh2Re[1] +
+                 (a.w23 - T(2) * a.w14 + a.w5) * co.oh2Re[2];
   return conv + diff;
 }
 
 template <typename T, int ST>
-__global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
+__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 4 : 2) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
                                                               int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot,
                                                               int kc) {
   constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
@@ -360,17 +375,16 @@ __global__ void __launch_bounds__(kTX *kTY) stage_kernel_tiled(Geometry g, Coeff
     for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
     const long q = g.idx(i, j, k);
     const unsigned hq = std::is_same<T, float>::value ? sr_mix((unsigned)q ^ salt) : 0u;
+    Taps<T> tp;
+    tp.load(A, kUseP);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
-      T r = rhs_tap(c, A, co);
+      T r = rhs_taps(c, tp, co);
       if (forcing) r = r + fe.eval(c, fx, fy, fz);
       T gp = T(0);
-      if (kUseP) {
-        const T pm = c == 0 ? A(3, -1, 0, 0) : (c == 1 ? A(3, 0, -1, 0) : A(3, 0, 0, -1));
-        gp = (A(3, 0, 0, 0) - pm) * co.oh[c];
-      }
-      const T self = A(c, 0, 0, 0);  // the input set's own value at the point
+      if (kUseP) gp = tp.dp(c) * co.oh[c];
+      const T self = tp.self(c);  // the input set's own value at the point
       // FP64 keeps the reference's expression order; the float path adds the
       // increment to the state with stochastic rounding
       constexpr bool kSR = std::is_same<T, float>::value;
