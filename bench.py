@@ -68,6 +68,9 @@ WORKLOADS = {
     # profiling case: ~1.5 GB on the device, z lines still DCT-I of 513 points
     "box256x256x512": ((257, 257, 513), (0.5, 0.5, 1.0), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
                        1e-4 * (64.0 / 512.0) ** 2, 1, 2),
+    # profiling case for the x sweeps of the 512^3 cube: x lines DCT-I of 513 points
+    "box512x256x256": ((513, 257, 257), (1.0, 0.5, 0.5), (0.0, 0.0, 0.0), (False, False, False), 1000.0,
+                       1e-4 * (64.0 / 512.0) ** 2, 1, 2),
 }
 
 # Algorithmic HBM sweeps (full-field reads + writes) per launch of each kernel
