@@ -358,6 +358,16 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 4 : 2) stage_kernel
     }
   };
   prefetch(kbeg);
+  // Per-thread invariants of the march: which components have (i, j) inside
+  // their interior, their last interior plane, and the (i, j) offset.
+  bool own_ij[3];
+  int klim[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    own_ij[c] = i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1;
+    klim[c] = g.ext(c, 2) - 1;
+  }
+  const long qij = (long)i + g.PX * (long)j;
   for (int k = kbeg; k < kend; ++k) {
     load_plane(k + 2);
     if (forcing) fz = fe.axis(2, k);
@@ -373,13 +383,13 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 4 : 2) stage_kernel
     Tap<T> A;
 #pragma unroll
     for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
-    const long q = g.idx(i, j, k);
+    const long q = qij + (long)k * sz;
     const unsigned hq = std::is_same<T, float>::value ? sr_mix((unsigned)q ^ salt) : 0u;
     Taps<T> tp;
     tp.load(A, kUseP);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      if (i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
+      if (!own_ij[c] || k >= klim[c]) continue;
       T r = rhs_taps(c, tp, co);
       if (forcing) r = r + fe.eval(c, fx, fy, fz);
       T gp = T(0);
