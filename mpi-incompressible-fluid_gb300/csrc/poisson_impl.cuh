@@ -301,7 +301,7 @@ __device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, 
   using T2 = typename Vec2<T>::type;
   const T h = T(0.5);
   for (int m = t; 2 * m <= L; m += stride) {
-    const int mn = (L - m) & (L - 1);
+    const int mn = m == 0 ? 0 : L - m;
     const T2 xm = row[m], xn = row[mn];
     T2 zm, zn;
     {
@@ -336,7 +336,8 @@ __device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row
                                                typename Vec2<T>::type &x1) {
   using T2 = typename Vec2<T>::type;
   const T2 xm = row[m], xn = row[N - m];
-  const T cp = T(kCos64[n1 * (32 / N1)]), sp = T(kSin64[n1 * (32 / N1)]);
+  static_assert(96 % N1 == 0, "pi n1 / N1 in the 192-entry table");
+  const T cp = T(kCos192[n1 * (96 / N1)]), sp = T(kSin192[n1 * (96 / N1)]);
   const T sn = sct.x * cp + sct.y * sp;  // sin(pi m / N)
   const T cs = sct.y * cp - sct.x * sp;  // cos(pi m / N)
   const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
@@ -461,7 +462,7 @@ template <typename T, int N1, int L>
 __device__ __forceinline__ void reg_twiddle_mul(typename Vec2<T>::type (&x)[N1], int t,
                                                 const typename Vec2<T>::type *tw) {
 #pragma unroll
-  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], __ldg(tw + ((t * k1) & (L - 1))));
+  for (int k1 = 1; k1 < N1; ++k1) x[k1] = cmul(x[k1], __ldg(tw + t * k1));  // t k1 < N2 N1 = L
 }
 
 // One length-L forward FFT (exponent sign -1) of the pair owned by this
@@ -509,10 +510,11 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
 
 // Three CTAs per SM (at most 80 registers) where the transform fits without
 // meaningful spills; the fused z sweep of the 32-point shapes keeps two (at
-// three it spills ~150 bytes and ran 8% slower on GB300).
+// three it spills ~150 bytes and ran 8% slower on GB300), and so do the
+// 48-point shapes (96 registers of data; their rows allow two CTAs anyway).
 template <int N1, int MODE>
 struct RegMinBlocks {
-  static constexpr int v = (MODE == 2 && N1 >= 32) ? 2 : 3;
+  static constexpr int v = (N1 >= 48 || (MODE == 2 && N1 >= 32)) ? 2 : 3;
 };
 
 template <typename T, int N1, int N2, int MODE, int KIND>
@@ -622,7 +624,7 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   const bool split = MODE == kModeForward && KIND == 1;
   auto value = [&](const T2 *r, int m, int comp) -> T {
     if (!split) return (comp ? r[m].y : r[m].x) * scale;
-    const T2 xm = r[m], xn = r[(L - m) & (L - 1)];
+    const T2 xm = r[m], xn = r[m == 0 ? 0 : L - m];
     const T h = T(0.5);
     if (2 * m <= L) return comp ? (xm.y + xn.y) * h : (xm.x + xn.x) * h;
     return comp ? (xm.x - xn.x) * h : (xn.y - xm.y) * h;
@@ -678,7 +680,7 @@ const void *reg_kernel_ptr(int mode, int kind) {
                                 : (const void *)line_kernel_reg<T, A, B, kModeFwdEigInv, 1>;
 }
 
-#define MIFGPU_REG_SHAPES(X) X(8, 8) X(16, 8) X(16, 16) X(32, 16) X(32, 32)
+#define MIFGPU_REG_SHAPES(X) X(8, 8) X(16, 8) X(16, 16) X(32, 16) X(32, 32) X(48, 8) X(48, 16)
 #ifndef MIFGPU_REG_TU
 #define MIFGPU_REG_EXTERN(A, B) extern template const void *reg_kernel_ptr<float, A, B>(int, int);
 MIFGPU_REG_SHAPES(MIFGPU_REG_EXTERN)
@@ -761,12 +763,17 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
   reg_n1 = reg_n2 = reg_L = 0;
   reg_half = false;
   const int cand = kind == 0 ? n - 1 : n;
-  if (std::is_same<T, float>::value && (cand & (cand - 1)) == 0 && cand >= 64 && cand <= 1024) {
+  const bool pow2_cand = (cand & (cand - 1)) == 0 && cand >= 64 && cand <= 1024;
+  if (std::is_same<T, float>::value && (pow2_cand || cand == 384 || cand == 768)) {
     reg_L = cand;
     reg_half = kind == 0;
-    int lg = 0;
-    while ((1 << lg) < reg_L) ++lg;
-    reg_n1 = 1 << ((lg + 1) / 2);
+    if (pow2_cand) {
+      int lg = 0;
+      while ((1 << lg) < reg_L) ++lg;
+      reg_n1 = 1 << ((lg + 1) / 2);
+    } else {
+      reg_n1 = 48;  // 3 x 2^k: 48 x 8 or 48 x 16
+    }
     reg_n2 = reg_L / reg_n1;
     reg_P = kThreads / reg_n2;
     reg_lg = 0;

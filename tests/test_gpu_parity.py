@@ -223,6 +223,10 @@ def test_poisson_solution_satisfies_discrete_laplacian(mifgpu_lib, cuda_device):
     ((65, 129, 33), (True, True, True)),      # real DFT lengths 64, 128, 32 (32: shared-memory path)
     ((257, 65, 513), (True, False, True)),    # channel-like: real DFT 256 / DCT 64 / real DFT 512
     ((17, 513, 9), (False, False, False)),    # register 512 along the strided y axis
+    ((769, 9, 5), (False, False, False)),     # register 768 = 48 x 16 (radix-3 base) along x
+    ((5, 9, 385), (False, False, False)),     # register 384 = 48 x 8, z fused
+    ((9, 769, 5), (False, True, False)),      # real DFT 768 along the strided y axis
+    ((9, 5, 385), (False, False, True)),      # real DFT 384, z fused
 ])
 def test_mixed_poisson_matches_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, periodic):
     """Mixed-precision Poisson solve (register FFT for power-of-two lengths)
