@@ -44,6 +44,8 @@ struct ImplBase {
   virtual void *field_ptr(int id) = 0;
   virtual int upload(mifgpu_ctx *ctx, int id, const double *host) = 0;
   virtual int download(mifgpu_ctx *ctx, int id, double *host) = 0;
+  virtual int upload_fields(mifgpu_ctx *ctx, const int *ids, const double *const *host, int count) = 0;
+  virtual int download_fields(mifgpu_ctx *ctx, const int *ids, double *const *host, int count) = 0;
   virtual int set_exact(mifgpu_ctx *ctx, int id, double t) = 0;
   virtual int step(mifgpu_ctx *ctx, int variant, const double *slots, int nsteps) = 0;
   virtual int apply_bc(mifgpu_ctx *ctx, int set, double t) = 0;
@@ -177,6 +179,15 @@ struct Impl final : ImplBase {
   double *acc = nullptr;    // device reduction scratch
   double *staging = nullptr;
   size_t staging_elems = 0;
+  // Host transfers of several fields at once (mifgpu_timestep_host): one
+  // reference-layout slot per field (slot 0 is `staging`), and copy streams
+  // that split each field's copy into chunks so several copy engines run at
+  // once while the scatter / gather kernels of other fields proceed.
+  static constexpr int kXferSlots = 4, kCopyStreams = 4;
+  double *xfer[kXferSlots] = {nullptr, nullptr, nullptr, nullptr};
+  size_t xfer_elems = 0;
+  cudaStream_t copy_stream[kCopyStreams] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t xfer_ev[kXferSlots + 1][kCopyStreams] = {};
   T *grad_block = nullptr;  // three fields for the pressure-gradient norm
   double *face_tab = nullptr;  // float path: the families' face data in double
   FaceTables ftabs{};
@@ -228,6 +239,12 @@ struct Impl final : ImplBase {
     for (auto &gx : rev_graph)
       if (gx) cudaGraphExecDestroy(gx);
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    for (int q = 1; q < kXferSlots; ++q) cudaFree(xfer[q]);
+    for (auto &row : xfer_ev)
+      for (auto &e : row)
+        if (e) cudaEventDestroy(e);
+    for (auto &cs : copy_stream)
+      if (cs) cudaStreamDestroy(cs);
   }
 
   int init(mifgpu_ctx *ctx) override {
@@ -328,24 +345,88 @@ struct Impl final : ImplBase {
     return MIFGPU_OK;
   }
 
-  int upload(mifgpu_ctx *ctx, int id, const double *host) override {
-    int e[3];
-    field_extent(g, id, e);
+  int upload(mifgpu_ctx *ctx, int id, const double *host) override { return upload_fields(ctx, &id, &host, 1); }
+
+  int download(mifgpu_ctx *ctx, int id, double *host) override { return download_fields(ctx, &id, &host, 1); }
+
+  // Slots and copy streams for `count` fields (created on first use).
+  int ensure_xfer(mifgpu_ctx *ctx, int count) {
     if (int rc = ensure_staging(ctx)) return rc;
-    const size_t n = (size_t)e[0] * e[1] * e[2];
-    CK(cudaMemcpyAsync(staging, host, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    launch_scatter<T>(g, F.f[id], staging, e[0], e[1], e[2], ctx->stream, &ctx->launches);
-    CK(cudaGetLastError());
+    const size_t need = staging_elems;
+    xfer[0] = staging;
+    for (int q = 1; q < count; ++q) {
+      if (xfer[q] && xfer_elems >= need) continue;
+      cudaFree(xfer[q]);
+      xfer[q] = nullptr;
+      if (cudaMalloc(&xfer[q], sizeof(double) * need) != cudaSuccess)
+        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of a transfer slot failed");
+      total_bytes += sizeof(double) * need;
+    }
+    if (count > 1) xfer_elems = need;
+    for (int c = 0; c < kCopyStreams; ++c) {
+      if (!copy_stream[c]) CK(cudaStreamCreateWithFlags(&copy_stream[c], cudaStreamNonBlocking));
+      for (auto &row : xfer_ev)
+        if (!row[c]) CK(cudaEventCreateWithFlags(&row[c], cudaEventDisableTiming));
+    }
     return MIFGPU_OK;
   }
 
-  int download(mifgpu_ctx *ctx, int id, double *host) override {
-    int e[3];
-    field_extent(g, id, e);
-    if (int rc = ensure_staging(ctx)) return rc;
-    const size_t n = (size_t)e[0] * e[1] * e[2];
-    launch_gather<T>(g, staging, F.f[id], e[0], e[1], e[2], ctx->stream, &ctx->launches);
-    CK(cudaMemcpyAsync(host, staging, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  // Bytes per copy chunk: large enough for full DMA efficiency, small enough
+  // that one field spreads over every copy stream.
+  static constexpr size_t kChunkElems = size_t(8) << 20;  // 64 MB of doubles
+
+  // Host (reference layout, double) -> fields `ids`: every field's copy is
+  // queued at once, in chunks spread over the copy streams, each field's
+  // scatter on the context stream after its chunks. The copies start after
+  // the context stream's earlier work (a slot may still feed a scatter).
+  int upload_fields(mifgpu_ctx *ctx, const int *ids, const double *const *host, int count) {
+    if (count < 1 || count > kXferSlots) return MIFGPU_EINVAL;
+    if (int rc = ensure_xfer(ctx, count)) return rc;
+    cudaEvent_t *start = xfer_ev[kXferSlots];
+    CK(cudaEventRecord(start[0], ctx->stream));
+    for (int c = 0; c < kCopyStreams; ++c) CK(cudaStreamWaitEvent(copy_stream[c], start[0], 0));
+    for (int q = 0; q < count; ++q) {
+      int e[3];
+      field_extent(g, ids[q], e);
+      const size_t n = (size_t)e[0] * e[1] * e[2];
+      int c = 0;
+      for (size_t off = 0; off < n; off += kChunkElems, c = (c + 1) % kCopyStreams) {
+        const size_t len = std::min(kChunkElems, n - off);
+        CK(cudaMemcpyAsync(xfer[q] + off, host[q] + off, sizeof(double) * len, cudaMemcpyHostToDevice,
+                           copy_stream[c]));
+      }
+      for (int cs = 0; cs < kCopyStreams; ++cs) {
+        CK(cudaEventRecord(xfer_ev[q][cs], copy_stream[cs]));
+        CK(cudaStreamWaitEvent(ctx->stream, xfer_ev[q][cs], 0));
+      }
+      launch_scatter<T>(g, F.f[ids[q]], xfer[q], e[0], e[1], e[2], ctx->stream, &ctx->launches);
+      CK(cudaGetLastError());
+    }
+    return MIFGPU_OK;
+  }
+
+  // Fields `ids` -> host: each field's gather on the context stream, its
+  // copy in chunks on the copy streams as soon as the gather is done;
+  // returns when every copy has landed.
+  int download_fields(mifgpu_ctx *ctx, const int *ids, double *const *host, int count) {
+    if (count < 1 || count > kXferSlots) return MIFGPU_EINVAL;
+    if (int rc = ensure_xfer(ctx, count)) return rc;
+    for (int q = 0; q < count; ++q) {
+      int e[3];
+      field_extent(g, ids[q], e);
+      const size_t n = (size_t)e[0] * e[1] * e[2];
+      launch_gather<T>(g, xfer[q], F.f[ids[q]], e[0], e[1], e[2], ctx->stream, &ctx->launches);
+      CK(cudaGetLastError());
+      CK(cudaEventRecord(xfer_ev[q][0], ctx->stream));
+      for (int c = 0; c < kCopyStreams; ++c) CK(cudaStreamWaitEvent(copy_stream[c], xfer_ev[q][0], 0));
+      int c = 0;
+      for (size_t off = 0; off < n; off += kChunkElems, c = (c + 1) % kCopyStreams) {
+        const size_t len = std::min(kChunkElems, n - off);
+        CK(cudaMemcpyAsync(host[q] + off, xfer[q] + off, sizeof(double) * len, cudaMemcpyDeviceToHost,
+                           copy_stream[c]));
+      }
+    }
+    for (int c = 0; c < kCopyStreams; ++c) CK(cudaStreamSynchronize(copy_stream[c]));
     CK(cudaStreamSynchronize(ctx->stream));
     return MIFGPU_OK;
   }
@@ -937,13 +1018,11 @@ int mifgpu_run(mifgpu_ctx *ctx, double t0, int nsteps) {
 int mifgpu_timestep_host(mifgpu_ctx *ctx, double t_n, double *u, double *v, double *w, double *p) {
   if (!ctx || !u || !v || !w || !p) return MIFGPU_EINVAL;
   double *h[4] = {u, v, w, p};
+  const double *hc[4] = {u, v, w, p};
   const int ids[4] = {0, 1, 2, kP};
-  for (int q = 0; q < 4; ++q)
-    if (int rc = ctx->impl->upload(ctx, ids[q], h[q])) return rc;
+  if (int rc = ctx->impl->upload_fields(ctx, ids, hc, 4)) return rc;
   if (int rc = mifgpu_timestep(ctx, t_n)) return rc;
-  for (int q = 0; q < 4; ++q)
-    if (int rc = ctx->impl->download(ctx, ids[q], h[q])) return rc;
-  return MIFGPU_OK;
+  return ctx->impl->download_fields(ctx, ids, h, 4);
 }
 
 int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n) {
