@@ -102,10 +102,13 @@ int mifgpu_field_extent(const mifgpu_ctx *ctx, int field, long out[3]);
 /* Host <-> device copies of one field in the reference layout (double).
  * upload is asynchronous on the context's stream: the host buffer must stay
  * valid until the next synchronising call. download returns after the data
- * has landed in `host`. The data travels as one DMA copy into a device
- * staging buffer and one layout kernel (measured on GB300: ~200 GB/s for
- * pinned and pageable buffers alike; kernels reading host memory directly
- * over NVLink-C2C were ~10% slower). */
+ * has landed in `host`. The data travels as DMA copies of 64 MB chunks,
+ * spread over four copy streams, into a device staging slot, and one layout
+ * kernel (mifgpu_timestep_host queues its four fields this way at once, so
+ * the copies of one field overlap the layout kernels of another). Measured
+ * on GB300 with pinned buffers: ~210 GB/s host to device and ~192 GB/s
+ * device to host, the link's per-direction rate for plain copies; kernels
+ * reading host memory directly over NVLink-C2C were ~10% slower. */
 int mifgpu_upload(mifgpu_ctx *ctx, int field, const double *host);
 int mifgpu_download(mifgpu_ctx *ctx, int field, double *host);
 
