@@ -272,8 +272,12 @@ __device__ __forceinline__ T rhs_taps(int c, const Taps<T> &a, const Coeffs<T> &
   return conv + diff;
 }
 
+// Float: six CTAs (48 warps) per SM at 40 registers, with a few dozen bytes
+// of spills; the march is latency bound (barriers, plane loads), and on
+// GB300 at 512^3 the stage time per step measured 5.30 / 5.48 / 4.80 / 4.61
+// / 4.48 / 4.75 ms for 2 / 3 / 4 / 5 / 6 / 8 CTAs per SM. FP64: two.
 template <typename T, int ST>
-__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 4 : 2) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
+__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 6 : 2) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
                                                               int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot,
                                                               int kc) {
   constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
