@@ -508,13 +508,13 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
   }
 }
 
-// Three CTAs per SM (at most 80 registers) where the transform fits without
-// meaningful spills; the fused z sweep of the 32-point shapes keeps two (at
-// three it spills ~150 bytes and ran 8% slower on GB300), and so do the
-// 48-point shapes (96 registers of data; their rows allow two CTAs anyway).
+// Three CTAs per SM (at most 80 registers; the rows of the 32 x 16 shape
+// allow three). The fused z sweep spills ~200 bytes at that bound but still
+// ran 2.5% faster on GB300 than at two CTAs (128 registers). The 48-point
+// shapes keep two (96 registers of data; their rows allow two CTAs anyway).
 template <int N1, int MODE>
 struct RegMinBlocks {
-  static constexpr int v = (N1 >= 48 || (MODE == 2 && N1 >= 32)) ? 2 : 3;
+  static constexpr int v = N1 >= 48 ? 2 : 3;
 };
 
 template <typename T, int N1, int N2, int MODE, int KIND>
