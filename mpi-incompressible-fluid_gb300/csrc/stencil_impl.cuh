@@ -832,7 +832,18 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches) {
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
   const int nk = g.Es[2] - 2;
-  const int kc = 32;  // planes per CTA
+  // Planes per CTA: 32, halved (down to 4) while the grid would not fill the
+  // GPU's resident slots (six CTAs per SM) once, so small grids still
+  // occupy every SM; every halving adds a plane of halo reads per CTA.
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+  }
+  const long tiles = (long)cdiv(ni - 2, kTX) * cdiv(g.Es[1] - 2, kTY);
+  int kc = 32;
+  while (kc > 4 && tiles * cdiv(nk, kc) < 6L * sms) kc /= 2;
   const dim3 tgrid(cdiv(ni - 2, kTX), cdiv(g.Es[1] - 2, kTY), cdiv(nk, kc));
   const double dt = sc.dt;
   StageCoef<T> K{};
