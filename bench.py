@@ -79,9 +79,12 @@ SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 2.0, "y_forward": 2.0, 
           "y_inverse": 2.0, "x_inverse": 2.0, "project": 9.0}
 LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3, "z_fused": 3, "y_inverse": 3,
                      "x_inverse": 3, "project": 3}
-# DRAM read + write bytes over algorithmic bytes, from one ncu capture of the
-# 256x256x512 profiling case (profiles/): applied to the full launch.
-MEASURED_TRAFFIC_RATIO = {"stage": 1.05, "y_forward": 0.83, "z_fused": 0.91, "y_inverse": 0.83, "x_inverse": 0.82}
+# DRAM read + write bytes over algorithmic bytes, from ncu captures of the
+# stage kernels on the 256x256x512 profiling case and of the line sweeps on
+# the 512x256x256 one: applied to the full launch. (The fused z sweep's
+# figure includes its 1/lambda table, one more field-sized read.)
+MEASURED_TRAFFIC_RATIO = {"stage": 1.07, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
+                          "x_inverse": 0.82}
 # Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps + 9 projection).
 STEP_SWEEPS = 102.0
 # The same step with the divergence fused into the x-forward sweep and the
@@ -649,9 +652,9 @@ def run_gpu(args):
     alg_bytes_launch = SWEEPS[dom] * elem * cells
     avg_launch_ms = classes[dom] / LAUNCHES_PER_STEP[dom]
     achieved = alg_bytes_launch / (avg_launch_ms / 1e3) / 1e9
-    # DRAM traffic per launch from one ncu capture of the same kernels on the
-    # 256x256x512 profiling case (profiles/stage_and_line_kernels_box256x256x512.md):
-    # measured read+write bytes over algorithmic bytes, applied to this launch.
+    # DRAM traffic per launch from one ncu capture of the same kernels on a
+    # profiling case: measured read+write bytes over algorithmic bytes,
+    # applied to this launch.
     ratio = MEASURED_TRAFFIC_RATIO.get(dom) if args.precision == "mixed" else None
     traffic = round(ratio * alg_bytes_launch) if ratio else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
