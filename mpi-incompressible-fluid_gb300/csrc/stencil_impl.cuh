@@ -179,7 +179,7 @@ struct StageCoef {
 // from shared memory and each point costs about five global loads.
 // Tile rows hold kTX + 2 used elements at a pitch of kTX + 4, so every row
 // starts 16-byte aligned and is copied with 16-byte cp.async.
-constexpr int kTX = 32, kTY = 8, kHX = kTX + 4, kHY = kTY + 2, kPL = kHX * kHY;
+constexpr int kTX = 32, kTY = 4, kHX = kTX + 4, kHY = kTY + 2, kPL = kHX * kHY;
 
 __device__ __forceinline__ void cp_async4_st(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -272,12 +272,14 @@ __device__ __forceinline__ T rhs_taps(int c, const Taps<T> &a, const Coeffs<T> &
   return conv + diff;
 }
 
-// Float: six CTAs (48 warps) per SM at 40 registers, with a few dozen bytes
-// of spills; the march is latency bound (barriers, plane loads), and on
-// GB300 at 512^3 the stage time per step measured 5.30 / 5.48 / 4.80 / 4.61
-// / 4.48 / 4.75 ms for 2 / 3 / 4 / 5 / 6 / 8 CTAs per SM. FP64: two.
+// Float: 48 warps per SM at 40 registers, with a few dozen bytes of spills;
+// the march is latency bound (barriers, plane loads). On GB300 at 512^3 the
+// stage time per step measured 5.30 / 5.48 / 4.80 / 4.61 / 4.48 / 4.75 ms for
+// 2 / 3 / 4 / 5 / 6 / 8 CTAs of 32 x 8 threads per SM, and 4.44 ms for twelve
+// CTAs of 32 x 4 (half the threads per barrier, 20 % more halo rows). FP64:
+// 8 warps per SM.
 template <typename T, int ST>
-__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 6 : 2) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
+__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
                                                               int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot,
                                                               int kc) {
   constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
@@ -835,7 +837,7 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
   const int nk = g.Es[2] - 2;
   // Planes per CTA: 32, halved (down to 4) while the grid would not fill the
-  // GPU's resident slots (six CTAs per SM) once, so small grids still
+  // GPU's resident slots (twelve CTAs per SM) once, so small grids still
   // occupy every SM; every halving adds a plane of halo reads per CTA.
   static int sms = 0;
   if (!sms) {
@@ -845,7 +847,7 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   }
   const long tiles = (long)cdiv(ni - 2, kTX) * cdiv(g.Es[1] - 2, kTY);
   int kc = 32;
-  while (kc > 4 && tiles * cdiv(nk, kc) < 6L * sms) kc /= 2;
+  while (kc > 4 && tiles * cdiv(nk, kc) < 12L * sms) kc /= 2;
   const dim3 tgrid(cdiv(ni - 2, kTX), cdiv(g.Es[1] - 2, kTY), cdiv(nk, kc));
   const double dt = sc.dt;
   StageCoef<T> K{};
