@@ -260,33 +260,59 @@ __global__ void div_adjoint_kernel(Geometry g, T *o0, T *o1, T *o2, const T *i0,
   }
 }
 
-// Adjoint of one periodic copy along axis d (src/StaggeredTensor.cpp:221-257):
-// forward a[0] = a[E-2], a[E-1] = a[1]; adjoint lam[1] += lam[E-1], lam[E-2] += lam[0],
-// then both ghosts cleared.
+// Adjoint of the periodic copies of all axes (src/StaggeredTensor.cpp:221-257).
+// Forward, along x, then y, then z: a[0] = a[E-2], a[E-1] = a[1]. The adjoint
+// runs z, y, x, and along one axis does lam[1] += lam[E-1],
+// lam[E-2] += lam[0], then clears both ghosts. Done at once as a gather:
+// every ghost value ends on one non-ghost point Q (its image along every
+// periodic axis where it is a ghost). The thread of Q sums the 2^n sources in
+// the sequential association,
+//   V_z(p) = lam(p) + lam(p, z ghost),  V_zy(p) = V_z(p) + V_z(p, y ghost),
+//   lam(Q) = V_zy(Q) + V_zy(Q, x ghost),
+// so the result is bitwise the one of the three passes, and then clears the
+// ghosts it read; no other thread reads them. blockIdx.z = comp * 6 + face:
+// Q on the face plane 1 / E-2 of periodic axis d, counted only on its first
+// such axis.
 template <typename T>
-__global__ void periodic_adjoint_kernel(Geometry g, T *f0, T *f1, T *f2, int d, int scalar) {
-  const int c = blockIdx.z;
+__global__ void periodic_fold_adjoint_kernel(Geometry g, T *f0, T *f1, T *f2, int scalar) {
+  const int c = blockIdx.z / 6, face = blockIdx.z % 6, d = face / 2, side = face % 2;
   T *f = c == 0 ? f0 : (c == 1 ? f1 : f2);
-  if (!f) return;
+  if (!f || !g.periodic[d]) return;
+  int ex[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) ex[ax] = scalar ? g.E[ax] : g.ext(c, ax);
   const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
-  auto ext = [&](int ax) { return scalar ? g.E[ax] : g.ext(c, ax); };
-  const long pa = blockIdx.x * blockDim.x + threadIdx.x;
-  const long pb = blockIdx.y * blockDim.y + threadIdx.y;
-  if (pa >= ext(a) || pb >= ext(b)) return;
-  const int E = ext(d);
-  long p[4][3];
-  const long dv[4] = {0, 1, E - 2, E - 1};
-  for (int r = 0; r < 4; ++r) {
-    p[r][a] = pa;
-    p[r][b] = pb;
-    p[r][d] = dv[r];
+  // the other two axes: non-ghost points of a periodic axis, all of another
+  const int la = g.periodic[a] ? 1 : 0, lb = g.periodic[b] ? 1 : 0;
+  const int na = g.periodic[a] ? ex[a] - 2 : ex[a], nb = g.periodic[b] ? ex[b] - 2 : ex[b];
+  const int pa = blockIdx.x * blockDim.x + threadIdx.x, pb = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pa >= na || pb >= nb) return;
+  int q[3];
+  q[d] = side == 0 ? 1 : ex[d] - 2;
+  q[a] = la + pa;
+  q[b] = lb + pb;
+  bool has[3];
+  int gh[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    has[ax] = g.periodic[ax] && (q[ax] == 1 || q[ax] == ex[ax] - 2);
+    gh[ax] = q[ax] == 1 ? ex[ax] - 1 : 0;
   }
-  const long q0 = g.idx(p[0][0], p[0][1], p[0][2]), q1 = g.idx(p[1][0], p[1][1], p[1][2]);
-  const long qm2 = g.idx(p[2][0], p[2][1], p[2][2]), qm1 = g.idx(p[3][0], p[3][1], p[3][2]);
-  f[q1] += f[qm1];
-  f[qm1] = T(0);
-  f[qm2] += f[q0];
-  f[q0] = T(0);
+  for (int ax = 0; ax < d; ++ax)
+    if (has[ax]) return;  // Q belongs to an earlier axis's face
+  // sources: bit ax of s set = coordinate ax replaced by its ghost
+  auto at = [&](int s) -> long {
+    const int x = (s & 1) ? gh[0] : q[0], y = (s & 2) ? gh[1] : q[1], z = (s & 4) ? gh[2] : q[2];
+    return g.idx(x, y, z);
+  };
+  auto vz = [&](int s) { return has[2] ? f[at(s)] + f[at(s | 4)] : f[at(s)]; };
+  auto vzy = [&](int s) { return has[1] ? vz(s) + vz(s | 2) : vz(s); };
+  const T v = has[0] ? vzy(0) + vzy(1) : vzy(0);
+  f[at(0)] = v;
+  for (int s = 1; s < 8; ++s) {
+    if (((s & 1) && !has[0]) || ((s & 2) && !has[1]) || ((s & 4) && !has[2])) continue;
+    f[at(s)] = T(0);
+  }
 }
 
 // Adjoint of the Dirichlet faces: those points were overwritten with data.
@@ -465,10 +491,9 @@ struct AdjointOps {
   static void bc_adjoint(const Geometry &g, T *const f[3], cudaStream_t s, long long *cnt) {
     int mx = 0;
     for (int d = 0; d < 3; ++d) mx = std::max(mx, g.Es[d]);
-    for (int d = 2; d >= 0; --d) {
-      if (!g.periodic[d]) continue;
-      adj::periodic_adjoint_kernel<T><<<dim3(adj::cdiv_u(mx, 32), adj::cdiv_u(mx, 8), 3), dim3(32, 8), 0, s>>>(
-          g, f[0], f[1], f[2], d, 0);
+    if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {
+      adj::periodic_fold_adjoint_kernel<T><<<dim3(adj::cdiv_u(mx, 32), adj::cdiv_u(mx, 8), 18), dim3(32, 8), 0, s>>>(
+          g, f[0], f[1], f[2], 0);
       ++*cnt;
     }
     if (!(g.periodic[0] && g.periodic[1] && g.periodic[2])) {
@@ -479,10 +504,9 @@ struct AdjointOps {
   static void periodic_scalar_adjoint(const Geometry &g, T *f, cudaStream_t s, long long *cnt) {
     int mx = 0;
     for (int d = 0; d < 3; ++d) mx = std::max(mx, g.E[d]);
-    for (int d = 2; d >= 0; --d) {
-      if (!g.periodic[d]) continue;
-      adj::periodic_adjoint_kernel<T><<<dim3(adj::cdiv_u(mx, 32), adj::cdiv_u(mx, 8), 1), dim3(32, 8), 0, s>>>(
-          g, f, nullptr, nullptr, d, 1);
+    if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {
+      adj::periodic_fold_adjoint_kernel<T><<<dim3(adj::cdiv_u(mx, 32), adj::cdiv_u(mx, 8), 6), dim3(32, 8), 0, s>>>(
+          g, f, nullptr, nullptr, 1);
       ++*cnt;
     }
   }
