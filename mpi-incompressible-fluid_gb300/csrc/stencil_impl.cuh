@@ -508,28 +508,38 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
   }
 }
 
-// Periodic ghost copy along axis d for up to three fields with their own
-// extents (src/StaggeredTensor.cpp:221-257): a[0] = a[E-2], a[E-1] = a[1].
+// Periodic copies of all axes at once (src/StaggeredTensor.cpp:221-257).
+// Along x, then y, then z the reference copies a[0] = a[E-2], a[E-1] = a[1]
+// over the whole face, ghosts of the other axes included; composed, every
+// ghost point ends equal to its image Q (each ghost coordinate 0 -> E-2,
+// E-1 -> 1), a non-ghost point, whatever the order. One thread per ghost
+// point copies f[Q] (reads non-ghost, writes ghost: no conflicts), so the
+// result is bitwise the three passes'. blockIdx.z = comp * 6 + face: the
+// ghost plane 0 / E-1 of periodic axis d, a point counted only on its first
+// ghost axis.
 template <typename T>
-__global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int d, int scalar) {
-  const int c = blockIdx.z;
+__global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int scalar) {
+  const int c = blockIdx.z / 6, face = blockIdx.z % 6, d = face / 2, side = face % 2;
   T *f = c == 0 ? f0 : (c == 1 ? f1 : f2);
-  if (!f) return;
+  if (!f || !g.periodic[d]) return;
+  int ex[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) ex[ax] = scalar ? g.E[ax] : g.ext(c, ax);
   const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
-  auto ext = [&](int ax) { return scalar ? g.E[ax] : g.ext(c, ax); };
-  const long pa = blockIdx.x * blockDim.x + threadIdx.x;
-  const long pb = blockIdx.y * blockDim.y + threadIdx.y;
-  if (pa >= ext(a) || pb >= ext(b)) return;
-  long lo[3], hi[3], src_lo[3], src_hi[3];
-  lo[a] = hi[a] = src_lo[a] = src_hi[a] = pa;
-  lo[b] = hi[b] = src_lo[b] = src_hi[b] = pb;
-  const int E = ext(d);
-  lo[d] = 0;
-  src_lo[d] = E - 2;
-  hi[d] = E - 1;
-  src_hi[d] = 1;
-  f[g.idx(lo[0], lo[1], lo[2])] = f[g.idx(src_lo[0], src_lo[1], src_lo[2])];
-  f[g.idx(hi[0], hi[1], hi[2])] = f[g.idx(src_hi[0], src_hi[1], src_hi[2])];
+  const int pa = blockIdx.x * blockDim.x + threadIdx.x, pb = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pa >= ex[a] || pb >= ex[b]) return;
+  int p[3];
+  p[d] = side == 0 ? 0 : ex[d] - 1;
+  p[a] = pa;
+  p[b] = pb;
+  int q[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    const bool ghost = g.periodic[ax] && (p[ax] == 0 || p[ax] == ex[ax] - 1);
+    if (ghost && ax < d) return;  // counted on an earlier axis's ghost plane
+    q[ax] = !ghost ? p[ax] : (p[ax] == 0 ? ex[ax] - 2 : 1);
+  }
+  f[g.idx(p[0], p[1], p[2])] = f[g.idx(q[0], q[1], q[2])];
 }
 
 // ---- Poisson right-hand side and projection ----
@@ -915,10 +925,9 @@ void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn
     bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft);
     if (launches) ++*launches;
   }
-  for (int d = 0; d < 3; ++d) {
-    if (!g.periodic[d]) continue;
-    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 3);
-    periodic_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], d, 0);
+  if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {
+    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 18);
+    periodic_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], 0);
     if (launches) ++*launches;
   }
 }
@@ -968,10 +977,9 @@ void launch_periodic_scalar(const Geometry &g, T *f, cudaStream_t s, long long *
   const dim3 blk(32, 8, 1);
   int mx = 0;
   for (int d = 0; d < 3; ++d) mx = mx > g.E[d] ? mx : g.E[d];
-  for (int d = 0; d < 3; ++d) {
-    if (!g.periodic[d]) continue;
-    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 1);
-    periodic_kernel<T><<<grid, blk, 0, s>>>(g, f, nullptr, nullptr, d, 1);
+  if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {
+    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 6);
+    periodic_kernel<T><<<grid, blk, 0, s>>>(g, f, nullptr, nullptr, 1);
     if (launches) ++*launches;
   }
 }
