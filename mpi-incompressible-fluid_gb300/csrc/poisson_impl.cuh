@@ -67,6 +67,9 @@ struct LineArgs {
   const typename Vec2<T>::type *dsc;  // register path, kind 2: (sin, cos)(pi j / N)
   int P, lg_lines;        // line pairs per CTA; log2(2P)
   int line_fast;          // 1: consecutive threads take consecutive lines (strided axes)
+  int vec16;              // x lines, register path, half-length DCT-I: 0, or the row pitch (floats)
+                          // of the 16-byte staging (every line starts 16-byte aligned and its row
+                          // holds the n points rounded up to 4)
   double scale;           // output multiplier (inverse normalisation), 1 otherwise
   // kModeFwdEigInv only: 1/(lambda_x + lambda_y + lambda_z) on the owner block,
   // z fastest, computed in double at set-up, zero mode 0.
@@ -269,6 +272,10 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
 }
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::); }
 
 // Element m of the first FFT's input for a real-DFT line pair: the plain
@@ -340,6 +347,29 @@ __device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row
   const T cp = T(kCos192[n1 * (96 / N1)]), sp = T(kSin192[n1 * (96 / N1)]);
   const T sn = sct.x * cp + sct.y * sp;  // sin(pi m / N)
   const T cs = sct.y * cp - sct.x * sp;  // cos(pi m / N)
+  const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
+  v.x = T(0.5) * sx - sn * dx;
+  v.y = T(0.5) * sy - sn * dy;
+  x1.x += cs * dx;
+  x1.y += cs * dy;
+}
+
+// The same from the 16-byte staging of contiguous x lines: the pair's two
+// lines a, b in consecutive staging rows.
+template <typename T, int N1>
+__device__ __forceinline__ void dct_half_input_staged(const T *la, const T *lb, int m, int n1, int N,
+                                                      typename Vec2<T>::type sct, typename Vec2<T>::type &v,
+                                                      typename Vec2<T>::type &x1) {
+  using T2 = typename Vec2<T>::type;
+  T2 xm, xn;
+  xm.x = la[m];
+  xm.y = lb[m];
+  xn.x = la[N - m];
+  xn.y = lb[N - m];
+  static_assert(96 % N1 == 0, "pi n1 / N1 in the 192-entry table");
+  const T cp = T(kCos192[n1 * (96 / N1)]), sp = T(kSin192[n1 * (96 / N1)]);
+  const T sn = sct.x * cp + sct.y * sp;
+  const T cs = sct.y * cp - sct.x * sp;
   const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
   v.x = T(0.5) * sx - sn * dx;
   v.y = T(0.5) * sy - sn * dy;
@@ -476,12 +506,18 @@ __device__ __forceinline__ void reg_twiddle_mul(typename Vec2<T>::type (&x)[N1],
 // phases are ordered by warp barriers.
 template <typename T, int N1, int N2, bool STORE = true>
 __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], typename Vec2<T>::type *row, int t,
-                                             const typename Vec2<T>::type *tw, bool conj_out) {
+                                             const typename Vec2<T>::type *tw, bool conj_out,
+                                             bool cta_first = false) {
   using T2 = typename Vec2<T>::type;
   constexpr int L = N1 * N2;
   RegDft<T2, N1, -1>::run(x);
   reg_twiddle_mul<T, N1, L>(x, t, tw);
-  __syncwarp();  // every thread of the pair has read its inputs from the row
+  // every thread of the pair has read its inputs from the row (with
+  // cta_first the inputs came from a CTA-wide staging the rows overlap)
+  if (cta_first)
+    __syncthreads();
+  else
+    __syncwarp();
 #pragma unroll
   for (int k1 = 0; k1 < N1; ++k1) row[k1 * (N2 + 1) + t] = x[k1];
   __syncwarp();
@@ -551,6 +587,21 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
     } else {
       for (int m = threadIdx.x >> a.lg_lines; m < n; m += ms) dst[2 * m] = T(0);
     }
+  } else if (KIND == 2 && MODE != kModeFwdEigInv && a.vec16) {
+    // Contiguous, 16-byte aligned x lines: line l in its own staging row of
+    // a.vec16 floats, 16-byte copies (the elements past n are read from the
+    // row padding and never used).
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5, nv = (n + 3) >> 2;
+    for (int l = threadIdx.x >> 5; l < nl; l += nw) {
+      const long off = table.off[l];
+      float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<T *>(smem_raw) + (long)l * a.vec16);
+      if (off >= 0) {
+        const float4 *src0 = reinterpret_cast<const float4 *>(a.data + off);
+        for (int v = lane; v < nv; v += 32) cp_async16(dst + v, src0 + v);
+      } else {
+        for (int v = lane; v < nv; v += 32) dst[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
   } else {
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int l = threadIdx.x >> 5; l < nl; l += nw) {
@@ -578,6 +629,8 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   cp_async_wait_all();
   __syncthreads();
   const T2 *src = row;
+  // (the fused z sweep's lines are always strided: no staging code there)
+  const bool staged = KIND == 2 && MODE != kModeFwdEigInv && !a.line_fast && a.vec16;
   const T *ea = nullptr, *eb = nullptr;
   if (MODE == kModeFwdEigInv) ea = a.eig + table.eoff[2 * pp] * n, eb = a.eig + table.eoff[2 * pp + 1] * n;
   constexpr int npass = MODE == kModeFwdEigInv ? 2 : 1;
@@ -600,7 +653,10 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
     for (int n1 = 0; n1 < N1; ++n1) {
       const int m = n1 * N2 + t;
       T2 v;
-      if (KIND == 2) {
+      if (KIND == 2 && staged && pass == 0) {
+        const T *lab = reinterpret_cast<const T *>(smem_raw) + (long)2 * pp * a.vec16;
+        dct_half_input_staged<T, N1>(lab, lab + a.vec16, m, n1, L, sct, v, x1);
+      } else if (KIND == 2) {
         dct_half_input<T, N1>(row, m, n1, L, sct, v, x1);
       } else {
         v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, L, MODE == kModeInverse)
@@ -610,7 +666,7 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
       x[n1] = v;
     }
     if constexpr (KIND == 2) {
-      reg_fft_core<T, N1, N2, false>(x, row, t, a.tw, false);
+      reg_fft_core<T, N1, N2, false>(x, row, t, a.tw, false, staged && pass == 0);
       const bool scale_eig = MODE == kModeFwdEigInv && pass == 0;
       dct_half_output<T, N1, N2>(x, row, t, x1, scale_eig ? ea : nullptr, scale_eig ? eb : nullptr);
     } else {
@@ -951,6 +1007,20 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
       a.tw = ax.reg_tw;
       a.dsc = ax.dsc;
       if (ax.reg_half) a.kind = 2;
+      a.vec16 = 0;
+      if (d == 0 && a.kind == 2) {
+        // 16-byte staging of the x lines: every line start 16-byte aligned
+        // (the strides are multiples of 8 elements), the rounded-up line
+        // inside its padded row, and the staging inside the kernel's rows.
+        // The pitch is a multiple of 4 with 2 x pitch = 16 mod 32 banks, so
+        // the two pairs of a warp read disjoint banks.
+        long pitch = (a.n + 3) / 4 * 4;
+        while (pitch % 16 != 8) pitch += 4;
+        const long nl = 2L * a.P;
+        const bool aligned = a.base % 4 == 0 && a.sa % 4 == 0 && a.sb % 4 == 0;
+        const bool in_row = (long)g.own_lo[0] + (a.n + 3) / 4 * 4 <= g.PX;
+        if (aligned && in_row && nl * pitch * (long)sizeof(T) <= (long)ax.reg_smem) a.vec16 = (int)pitch;
+      }
       const unsigned grid = (unsigned)((total + 2 * a.P - 1) / (2 * a.P));
       launch_reg<T>(ax.reg_n1, ax.reg_n2, mode, grid, ax.reg_smem, stream, a);
       if (launches) ++*launches;
