@@ -1,7 +1,7 @@
 """ctypes bindings to the oracle libraries — TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
-this module, and only as the checker. Two libraries:
+this module, and only to check results against. Two libraries:
 
 * ``RefSolver``   — oracle/_ref/libmifref.so: the reference's own sources
   compiled here against single-rank MPI / FFTW stand-ins (oracle/Makefile,

@@ -12,7 +12,7 @@ gradient is checked against the library's own forward map, in FP64, by
     eps = 1e-6),
   * the derivative with respect to the Taylor-Green forcing amplitude
     (step 1e-4),
-each to a relative error of 1e-6 (the benchmark spec's bound), on a periodic box,
+each to a relative error of 1e-6 (the required bound), on a periodic box,
 an all-Dirichlet box with time-dependent wall data and a channel. The FP32
 adjoint is compared with the FP64 one; the checkpoint interval must not
 change the result; the autograd wrapper must return the same gradient.

@@ -1,7 +1,7 @@
 """GPU parity of the CUDA library against the oracle, through the C ABI.
 
 FP64 mode must match within 1e-12 normwise per field (max|gpu - cpu| /
-max|cpu|), the benchmark spec's tolerance: the GPU evaluates the same expressions
+max|cpu|), the required tolerance: the GPU evaluates the same expressions
 but may fuse multiply-adds and uses its own FFT, so bits differ by rounding.
 Mixed mode is compared with the FP64 oracle at a float tolerance.
 
