@@ -85,6 +85,10 @@ LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3
 # figure includes its 1/lambda table, one more field-sized read.)
 MEASURED_TRAFFIC_RATIO = {"stage": 1.07, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
                           "x_inverse": 0.82}
+# FP64 operations of one FP64 step per cell (an FMA counted as two), from the
+# DFMA / DADD / DMUL instruction counters of an ncu capture of the
+# 256x256x512 case; the 512^3 step's longer x and y transforms add a few per cent.
+FP64_FLOPS_PER_CELL_STEP = 1249.0
 # Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps + 9 projection).
 STEP_SWEEPS = 102.0
 # The same step with the divergence fused into the x-forward sweep and the
@@ -736,6 +740,16 @@ def run_gpu(args):
         ms64 = a0.elapsed_time(a1) / n64
         fp64 = {"ms_per_step": round(ms64, 3), "value": cells / (ms64 / 1e3) / 1e9,
                 "mixed_speedup": round(ms64 / step_ms, 2)}
+        # both rooflines of the FP64 step: the FP64 pipe (its FMA rate probed
+        # live) and HBM (the as-built sweeps at 8 bytes)
+        peak64 = mifgpu.probe_fp64_fma()
+        flops = FP64_FLOPS_PER_CELL_STEP * cells / (ms64 / 1e3) / 1e12
+        fp64["fp64_alu_roofline"] = {"achieved_tflops": round(flops, 4), "peak_tflops": round(peak64, 4),
+                                     "frac": round(flops / peak64, 4),
+                                     "flops_per_cell_step": FP64_FLOPS_PER_CELL_STEP,
+                                     "peak_source": "FMA-chain probe (mifgpu_probe_fp64_fma)"}
+        fp64["hbm_roofline"] = {"achieved_gbs": round(STEP_SWEEPS * 8 * cells / (ms64 / 1e3) / 1e9, 1),
+                                "peak_gbs": peak, "frac": round(STEP_SWEEPS * 8 * cells / (ms64 / 1e3) / 1e9 / peak, 4)}
         s64.run((1 + n64) * dt, max(0, args.warmup + args.steps - 1 - n64))
         if kind != 0:
             t64 = (args.warmup + args.steps) * dt

@@ -270,6 +270,13 @@ int mifgpu_launch_count(const mifgpu_ctx *ctx, long long *out);
 /* Device bytes held by the context. */
 int mifgpu_device_bytes(const mifgpu_ctx *ctx, size_t *out);
 
+/* No counterpart in the reference (instrumentation). The FP64 fused
+ * multiply-add rate of the current device in TFLOP/s (an FMA counted as two
+ * operations): independent FMA chains on every SM, timed with CUDA events
+ * after one warm-up launch. It is the FP64-pipe ceiling of a plain FP64 step,
+ * beside the HBM one. Needs no context; synchronises the device. */
+int mifgpu_probe_fp64_fma(double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

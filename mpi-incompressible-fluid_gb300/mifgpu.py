@@ -35,7 +35,7 @@ EXPORTED = [
     "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_profile_step", "mifgpu_launch_count",
     "mifgpu_device_bytes", "mifgpu_gradient_ke", "mifgpu_backward", "mifgpu_download_adjoint",
     "mifgpu_set_forcing_amplitude", "mifgpu_velocity_error_norms_noalloc", "mifgpu_write_vtk",
-    "mifgpu_write_dat", "mifgpu_write_vtk_full_mesh",
+    "mifgpu_write_dat", "mifgpu_write_vtk_full_mesh", "mifgpu_probe_fp64_fma",
 ]
 PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
                    "x_inverse", "periodic", "project"]
@@ -104,6 +104,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_write_vtk": [vp, C.c_char_p],
         "mifgpu_write_dat": [vp, C.c_char_p, i, d, d, d],
         "mifgpu_write_vtk_full_mesh": [vp, C.c_char_p],
+        "mifgpu_probe_fp64_fma": [dp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -113,6 +114,16 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.mifgpu_last_error.restype = C.c_char_p
     _LIB = lib
     return lib
+
+
+def probe_fp64_fma() -> float:
+    """FP64 fused multiply-add rate of the current device, TFLOP/s (instrumentation)."""
+    lib = load_library()
+    out = C.c_double(0.0)
+    rc = lib.mifgpu_probe_fp64_fma(C.byref(out))
+    if rc != 0:
+        raise MifGpuError(f"mifgpu_probe_fp64_fma failed ({rc})")
+    return out.value
 
 
 class Solver:
