@@ -717,6 +717,25 @@ def run_gpu(args):
         e2e = {"value": world * cells * k_e2e / el / 1e9, "unit": UNIT, "h2d_bytes_per_step": bi,
                "d2h_bytes_per_step": bi, "steps": k_e2e, "api": "mifgpu_timestep_host",
                "host_buffers": "pinned, allocated after binding to " + affinity}
+        # The host link measured on the same buffers with plain copies (one
+        # device tensor per field), and the e2e rate it allows: the step plus
+        # both transfers at those rates, nothing overlapped.
+        dev = {nm: torch.empty_like(host[nm], device="cuda") for nm in names}
+        rates = {}
+        for direction in ("h2d", "d2h"):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for nm in names:
+                if direction == "h2d":
+                    dev[nm].copy_(host[nm], non_blocking=True)
+                else:
+                    host[nm].copy_(dev[nm], non_blocking=True)
+            torch.cuda.synchronize()
+            rates[direction] = bi / (time.perf_counter() - t0) / 1e9
+        del dev
+        ceiling_s = step_ms / 1e3 + bi / (rates["h2d"] * 1e9) + bi / (rates["d2h"] * 1e9)
+        e2e["link_gbs"] = {k: round(v, 1) for k, v in rates.items()}
+        e2e["link_bound_value"] = round(world * cells / ceiling_s / 1e9, 4)
         del np
 
     # FP64 comparison point on the same workload (fewer steps; FP64 is ALU-bound on GB300)
