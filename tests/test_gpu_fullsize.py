@@ -1,0 +1,38 @@
+"""The benchmark's full size (the 512^3 Ethier-Steinman cube, 513^3 nodes),
+checked through properties that do not need the oracle at that size: two
+steps in FP64 and in mixed precision each stay within their known distance
+of the exact solution (FP64 8.0e-7 and mixed 1.3e-6 in L-infinity at this
+dt), and the mixed fields stay within float rounding of the FP64 ones. The
+FP64 path itself is pinned to the oracle on the smaller grids."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 513
+DT = 1e-4 * (64.0 / 512.0) ** 2
+
+
+def run(mg, precision):
+    s = mg.Solver(n_global=(N, N, N), Re=1000.0, dt=DT, precision=precision, boundary_kind=mg.FIELD_ETHIER)
+    s.set_exact_velocity(0, 0.0)
+    s.set_exact_pressure(0.0)
+    s.run(0.0, 2)
+    s.adjust_pressure(2 * DT)
+    norms = s.error_norms(2 * DT)
+    fields = {n: s.download(n) for n in ("u", "w", "p")}
+    s.close()
+    return norms, fields
+
+
+def test_full_size_steps_fp64_and_mixed(mifgpu_lib, cuda_device):
+    n64, f64 = run(mifgpu_lib, mifgpu_lib.FP64)
+    nmx, fmx = run(mifgpu_lib, mifgpu_lib.MIXED)
+    # velocity L-infinity against the exact solution (norms[2])
+    assert n64[2] < 1.0e-6, n64[2]
+    assert nmx[2] < 3.0e-6, nmx[2]
+    for n in ("u", "w"):
+        scale = np.abs(f64[n]).max()
+        assert np.abs(fmx[n] - f64[n]).max() <= 1e-5 * scale, n
+    scale = np.abs(f64["p"]).max()
+    assert np.abs(fmx["p"] - f64["p"]).max() <= 1e-3 * scale
