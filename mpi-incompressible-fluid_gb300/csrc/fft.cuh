@@ -37,6 +37,12 @@ __device__ __forceinline__ T2 csub(T2 a, T2 b) {
   r.y = a.y - b.y;
   return r;
 }
+// FP32 complex add and subtract as one packed FP32x2 instruction each (each
+// lane rounds as the scalar operation would: a - b is fma(b, -1, a), one
+// rounding of the exact difference).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
 // a * (i * sign)
 template <typename T2>
 __device__ __forceinline__ T2 cmul_isign(T2 a, int sign) {
