@@ -337,21 +337,27 @@ __device__ __forceinline__ void reg_eig_row(typename Vec2<T>::type *row, int t, 
 // X_1. (sin, cos)(pi m / N) comes from the thread's own angle pi t / N
 // (sct, from the table) and the compile-time angle pi n1 / N1 by the
 // angle-addition formulas.
+// The half-length DCT-I input arithmetic on the pair (packed FP32x2):
+// s = xm + xn, d = xm - xn, v = s/2 - sin(pi m/N) d, x1 += cos(pi m/N) d, with
+// (sin, cos)(pi m / N) from the thread's angle sct and the compile-time
+// angle pi n1 / N1, each formed as a pair holding the value twice.
+template <int N1>
+__device__ __forceinline__ void dct_half_pre(float2 xm, float2 xn, int n1, float2 sct, float2 &v, float2 &x1) {
+  static_assert(96 % N1 == 0, "pi n1 / N1 in the 192-entry table");
+  const float cp = float(kCos192[n1 * (96 / N1)]), sp = float(kSin192[n1 * (96 / N1)]);
+  const float2 sxx = make_float2(sct.x, sct.x), syy = make_float2(sct.y, sct.y);
+  const float2 nsn = __ffma2_rn(syy, make_float2(-sp, -sp), __fmul2_rn(sxx, make_float2(-cp, -cp)));  // -sin
+  const float2 cs = __ffma2_rn(sxx, make_float2(-sp, -sp), __fmul2_rn(syy, make_float2(cp, cp)));    // cos
+  const float2 sm = cadd(xm, xn), d = csub(xm, xn);
+  v = __ffma2_rn(nsn, d, __fmul2_rn(make_float2(0.5f, 0.5f), sm));
+  x1 = __ffma2_rn(cs, d, x1);
+}
+
 template <typename T, int N1>
 __device__ __forceinline__ void dct_half_input(const typename Vec2<T>::type *row, int m, int n1, int N,
                                                typename Vec2<T>::type sct, typename Vec2<T>::type &v,
                                                typename Vec2<T>::type &x1) {
-  using T2 = typename Vec2<T>::type;
-  const T2 xm = row[m], xn = row[N - m];
-  static_assert(96 % N1 == 0, "pi n1 / N1 in the 192-entry table");
-  const T cp = T(kCos192[n1 * (96 / N1)]), sp = T(kSin192[n1 * (96 / N1)]);
-  const T sn = sct.x * cp + sct.y * sp;  // sin(pi m / N)
-  const T cs = sct.y * cp - sct.x * sp;  // cos(pi m / N)
-  const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
-  v.x = T(0.5) * sx - sn * dx;
-  v.y = T(0.5) * sy - sn * dy;
-  x1.x += cs * dx;
-  x1.y += cs * dy;
+  dct_half_pre<N1>(row[m], row[N - m], n1, sct, v, x1);
 }
 
 // The same from the 16-byte staging of contiguous x lines: the pair's two
@@ -360,21 +366,7 @@ template <typename T, int N1>
 __device__ __forceinline__ void dct_half_input_staged(const T *la, const T *lb, int m, int n1, int N,
                                                       typename Vec2<T>::type sct, typename Vec2<T>::type &v,
                                                       typename Vec2<T>::type &x1) {
-  using T2 = typename Vec2<T>::type;
-  T2 xm, xn;
-  xm.x = la[m];
-  xm.y = lb[m];
-  xn.x = la[N - m];
-  xn.y = lb[N - m];
-  static_assert(96 % N1 == 0, "pi n1 / N1 in the 192-entry table");
-  const T cp = T(kCos192[n1 * (96 / N1)]), sp = T(kSin192[n1 * (96 / N1)]);
-  const T sn = sct.x * cp + sct.y * sp;
-  const T cs = sct.y * cp - sct.x * sp;
-  const T sx = xm.x + xn.x, sy = xm.y + xn.y, dx = xm.x - xn.x, dy = xm.y - xn.y;
-  v.x = T(0.5) * sx - sn * dx;
-  v.y = T(0.5) * sy - sn * dy;
-  x1.x += cs * dx;
-  x1.y += cs * dy;
+  dct_half_pre<N1>(make_float2(la[m], lb[m]), make_float2(la[N - m], lb[N - m]), n1, sct, v, x1);
 }
 
 // Z of the pair in registers (x[r*N2 + k2] = Z_k, k = t + N2 (r + R k2),
@@ -413,8 +405,7 @@ __device__ __forceinline__ void dct_half_output(const typename Vec2<T>::type (&x
     zn.x = __shfl_sync(0xffffffffu, send.x, partner, N2);
     zn.y = __shfl_sync(0xffffffffu, send.y, partner, N2);
     if (t == 0) zn = c == 0 ? zk : x[reg(N1 - c)];
-    ev[c].x = zk.x + zn.x;
-    ev[c].y = zk.y + zn.y;
+    ev[c] = cadd(zk, zn);
     const bool k0 = c == 0 && t == 0;
     T2 d;
     d.x = k0 ? T(0) : zn.y - zk.y;
@@ -426,9 +417,7 @@ __device__ __forceinline__ void dct_half_output(const typename Vec2<T>::type (&x
   T2 run = {T(0), T(0)};
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const T2 d = row[pad(t * C + c)];
-    run.x += d.x;
-    run.y += d.y;
+    run = cadd(run, row[pad(t * C + c)]);
     dd[c] = run;
   }
   T2 incl = run;
@@ -447,12 +436,7 @@ __device__ __forceinline__ void dct_half_output(const typename Vec2<T>::type (&x
   if (t == 0) excl.x = excl.y = T(0);
   __syncwarp();
 #pragma unroll
-  for (int c = 0; c < C; ++c) {
-    T2 o;
-    o.x = x1.x + (excl.x + dd[c].x);
-    o.y = x1.y + (excl.y + dd[c].y);
-    row[pad(t * C + c)] = o;
-  }
+  for (int c = 0; c < C; ++c) row[pad(t * C + c)] = cadd(x1, cadd(excl, dd[c]));
   __syncwarp();
   // D: the odd outputs back in the strided order
 #pragma unroll
