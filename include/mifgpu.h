@@ -86,7 +86,17 @@ typedef struct mifgpu_ctx mifgpu_ctx;
 
 /* Replaces the set-up of src/main.cpp:127-141: Constants,
  * PressureSolverStructures (src/PressureSolverStructures.cpp:13-70) and the
- * six tensors. All fields start at zero. */
+ * six tensors. All fields start at zero.
+ * Returns MIFGPU_EINVAL, with *out left NULL and no device work done, for
+ * parameters out of range:
+ *   - fewer than 3 points on an axis;
+ *   - a staggered extent above the CUDA grid limits of the box kernels,
+ *     where the staggered extent is n_global + 1 on a Dirichlet axis and
+ *     n_global + 2 on a periodic y or z axis: z above 65535, y above
+ *     262140, any axis above 524280.
+ * A Poisson line longer than the shared-memory transforms hold returns
+ * MIFGPU_ENOTSUP with a context whose mifgpu_last_error() says so; the
+ * caller destroys it. */
 int mifgpu_create(const mifgpu_params *params, mifgpu_ctx **out);
 int mifgpu_destroy(mifgpu_ctx *ctx);
 

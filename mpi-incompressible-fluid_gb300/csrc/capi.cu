@@ -923,6 +923,14 @@ int mifgpu_create(const mifgpu_params *p, mifgpu_ctx **out) {
   g.Es[0] = g.periodic[0] ? g.E[0] : g.E[0] + 1;
   g.Es[1] = g.E[1] + 1;
   g.Es[2] = g.E[2] + 1;
+  // CUDA grids hold at most 65535 blocks along y and z. The box kernels give
+  // every z plane of a staggered field its own grid-z block, the stencil
+  // kernels tile y in rows of 4, and the face kernels tile the longest
+  // extent in rows of 8. A longer axis is refused here, before any device
+  // work, instead of failing at its first launch.
+  constexpr long kGridYZ = 65535;
+  if (g.Es[2] > kGridYZ || g.Es[1] > 4 * kGridYZ || std::max({g.Es[0], g.Es[1], g.Es[2]}) > 8 * kGridYZ)
+    return MIFGPU_EINVAL;
   g.PX = ((long)std::max(g.Es[0], g.E[0]) + 7) / 8 * 8;
   g.PY = g.Es[1];
   g.PZ = g.Es[2];

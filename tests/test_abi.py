@@ -48,6 +48,10 @@ def _params(mg, **kw):
     dict(precision=7),
     dict(kind=9),
     dict(forcing=-1),
+    dict(n=(9, 9, 65535)),      # staggered z extent 65536: above grid z
+    dict(n=(9, 9, 65534), periodic=(0, 0, 1)),  # periodic z: extent n + 2
+    dict(n=(9, 262140, 9)),     # staggered y extent above 4 rows x 65535
+    dict(n=(524280, 9, 9)),     # x above the face kernels' 8 x 65535
 ])
 def test_create_rejects_invalid_parameters_without_a_device(mifgpu_lib, bad):
     lib = mifgpu_lib.load_library()
@@ -55,6 +59,26 @@ def test_create_rejects_invalid_parameters_without_a_device(mifgpu_lib, bad):
     h = C.c_void_p()
     assert lib.mifgpu_create(C.byref(p), C.byref(h)) == -1
     assert not h.value
+
+
+@pytest.mark.parametrize("good", [
+    dict(n=(9, 9, 65534)),                      # staggered z extent 65535
+    dict(n=(9, 9, 65533), periodic=(0, 0, 1)),  # periodic z: 65533 + 2
+    dict(n=(9, 262139, 9)),                     # staggered y extent 262140
+])
+def test_create_accepts_the_largest_grid_extents(mifgpu_lib, good):
+    """At the grid limits the parameter check passes. What follows depends
+    on the machine: without a device, create fails at the device query
+    (MIFGPU_ECUDA). With one, the long Poisson lines are refused
+    (MIFGPU_ENOTSUP) or the context is built. None of these is
+    MIFGPU_EINVAL."""
+    lib = mifgpu_lib.load_library()
+    p = _params(mifgpu_lib, **good)
+    h = C.c_void_p()
+    rc = lib.mifgpu_create(C.byref(p), C.byref(h))
+    if h.value:
+        lib.mifgpu_destroy(h)
+    assert rc != -1
 
 
 def test_null_arguments_are_rejected(mifgpu_lib):
