@@ -545,6 +545,15 @@ static void project(St *s, int set, double dt_k) {
   }
 }
 
+/* The pair the step runs after each Poisson solve, as one call. */
+int mif_oracle_project(void *h, int set, double dt) {
+  St *s = (St *)h;
+  if (set < 0 || set > 2) return -1;
+  update_pressure(s);
+  project(s, set, dt);
+  return 0;
+}
+
 /* src/Timestep.cpp:97-156 */
 static void full_step(St *s, double t_n, int nhn) {
   const double dt_1 = 64.0 / 120.0 * s->dt;

@@ -49,6 +49,9 @@ int mif_oracle_timestep_velocity(void *h, double t_n);
 int mif_oracle_solve_pressure(void *h, int set, double dt);
 int mif_oracle_solve_pressure_nhn(void *h, int set, double dt, double t_new, double t_old);
 int mif_oracle_apply_bc(void *h, int set, double t);
+/* p += phi, then u -= dt grad(phi) on velocity set `set` (interior points):
+ * update_pressure + update_velocity_pressure_gradient, src/Timestep.cpp:66-81 */
+int mif_oracle_project(void *h, int set, double dt);
 int mif_oracle_adjust_pressure(void *h, double t);
 int mif_oracle_error_norms(void *h, double t, double out[9]);
 double mif_oracle_forcing_value(int kind, int comp, double t, double x, double y, double z, double Re, int with_p);

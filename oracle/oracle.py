@@ -117,7 +117,7 @@ class _Solver:
             fn = getattr(self.lib, pre + name)
             fn.argtypes = [C.c_void_p, C.c_double]
             fn.restype = C.c_int
-        for name in ("solve_pressure", "apply_bc"):
+        for name in ("solve_pressure", "apply_bc", "project"):
             fn = getattr(self.lib, pre + name)
             fn.argtypes = [C.c_void_p, C.c_int, C.c_double]
             fn.restype = C.c_int
@@ -186,6 +186,9 @@ class _Solver:
 
     def apply_bc(self, vset: int, t: float):
         assert self._fn("apply_bc")(self.h, vset, t) == 0
+
+    def project(self, vset: int, dt: float):
+        assert self._fn("project")(self.h, vset, dt) == 0
 
     def adjust_pressure(self, t: float):
         assert self._fn("adjust_pressure")(self.h, t) == 0

@@ -33,9 +33,13 @@
 // include/Timestep.h and include/TimestepVelocity.h share the include guard
 // TIMESTEP_VELOCITY_H, so only one of them can be included per translation
 // unit; this repeats the declaration of include/TimestepVelocity.h:15-16.
+// src/Timestep.cpp:66-81 defines the two projection helpers with external
+// linkage but no header declares them; these lines repeat their signatures.
 namespace mif {
 void timestep_velocity(VelocityTensor &velocity, VelocityTensor &velocity_buffer, VelocityTensor &rhs_buffer,
                        const TimeVectorFunction &exact_velocity, Real t_n);
+void update_velocity_pressure_gradient(VelocityTensor &velocity, const StaggeredTensor &pressure, Real delta_time);
+void update_pressure(StaggeredTensor &pressure, const StaggeredTensor &pressure_difference);
 }
 
 // Globals the reference's generated headers declare (include/Manufactured*.h).
@@ -192,6 +196,17 @@ int mifref_solve_pressure_nhn(void *h, int set, double dt, double t_new, double 
   mif::solve_pressure_equation_non_homogeneous_neumann(
       *s->pressure_buffer, *s->solver_buffer, *s->vel[set],
       s->exact_pressure_gradient->get_difference_over_time(t_new, t_old), dt);
+  return 0;
+}
+
+// Pressure accumulation and gradient correction on velocity set `set`, the
+// pair the step runs after each Poisson solve: update_pressure then
+// update_velocity_pressure_gradient (src/Timestep.cpp:66-81; both have
+// external linkage there, no header declares them).
+int mifref_project(void *h, int set, double dt) {
+  auto *s = static_cast<RefState *>(h);
+  mif::update_pressure(*s->pressure, *s->pressure_buffer);
+  mif::update_velocity_pressure_gradient(*s->vel[set], *s->pressure_buffer, dt);
   return 0;
 }
 

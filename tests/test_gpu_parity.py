@@ -141,6 +141,33 @@ def test_fp64_steps_match_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, per
         assert err <= max(FP64_TOL, 4.0 * sens[n]), f"{n}: {err:.3e} (oracle one-ulp sensitivity {sens[n]:.3e})"
 
 
+@pytest.mark.parametrize("shape,periodic", [
+    ((9, 8, 7), (False, False, False)),
+    ((8, 9, 10), (True, True, True)),
+    ((9, 7, 8), (True, False, True)),
+    ((7, 8, 9), (False, True, False)),
+])
+def test_project_matches_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, periodic):
+    """mifgpu_project on its own (p += phi, then u -= dt grad(phi) on the
+    interior of one velocity set, src/Timestep.cpp:66-81). Every field is
+    random, ghosts included, so the points it must leave alone are checked
+    too."""
+    kw = dict(n_global=shape, size=(1.0, 1.2, 2.0), origin=(0.0, -0.5, -1.0), Re=800.0, dt=2e-4,
+              periodic=periodic, exact_kind=0)
+    o = oracle_lib.OracleSolver(oracle_lib.Case(**kw))
+    rng = np.random.default_rng(17)
+    for n in oracle_lib.FIELD_NAMES:
+        o.set(n, rng.standard_normal(o.shape(n)))
+    g = make_solver(mifgpu_lib, kw)
+    g.load_state({n: o.get(n) for n in oracle_lib.FIELD_NAMES})
+    o.project(1, 3.7e-4)
+    g.project(1, 3.7e-4)
+    for n in oracle_lib.FIELD_NAMES:
+        err = rel_err(g.download(n), o.get(n))
+        assert err <= FP64_TOL, f"{n}: {err:.3e}"
+    g.close()
+
+
 def test_contexts_of_different_sizes_coexist(oracle_lib, mifgpu_lib, cuda_device):
     """A context whose line kernels need more dynamic shared memory keeps
     working after a smaller context was created (the kernel attribute is

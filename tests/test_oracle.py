@@ -123,6 +123,33 @@ def test_oracle_bit_exact_against_reference_library(oracle_lib):
         assert np.array_equal(r.get(n), o.get(n)), n
 
 
+@pytest.mark.parametrize("shape,periodic", [
+    ((9, 8, 7), (False, False, False)),
+    ((8, 9, 10), (True, True, True)),
+    ((9, 7, 8), (True, False, True)),
+    ((7, 8, 9), (False, True, False)),
+])
+def test_oracle_project_bit_exact_against_reference_library(oracle_lib, shape, periodic):
+    """p += phi and u -= dt grad(phi) on a velocity set, against the
+    reference's update_pressure and update_velocity_pressure_gradient
+    (src/Timestep.cpp:66-81). Every field, ghosts included, is random."""
+    O = oracle_lib
+    if not O.RefSolver.available():
+        pytest.skip("reference library not built here (no reference sources)")
+    case = O.Case(n_global=shape, size=(1.0, 1.2, 2.0), origin=(0.0, -0.5, -1.0), Re=800.0, dt=2e-4,
+                  periodic=periodic)
+    r, o = O.RefSolver(case), O.OracleSolver(case)
+    rng = np.random.default_rng(17)
+    for n in O.FIELD_NAMES:
+        a = rng.standard_normal(o.shape(n))
+        r.set(n, a)
+        o.set(n, a)
+    for s in (r, o):
+        s.project(1, 3.7e-4)
+    for n in O.FIELD_NAMES:
+        assert np.array_equal(r.get(n), o.get(n)), n
+
+
 def test_forcing_formula_matches_symbolic_residual(oracle_lib):
     """The hand-written SINCOS forcing equals u_t + (u.grad)u - lap(u)/Re (+grad p)
     derived symbolically, the construction of generators/manufsol_velocity.py."""
