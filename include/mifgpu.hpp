@@ -105,6 +105,91 @@ class Solver {
   }
   void set_exact_velocity(int set, double t) { check(mifgpu_set_exact_velocity(ctx_, set, t), "set_exact_velocity"); }
   void set_exact_pressure(double t) { check(mifgpu_set_exact_pressure(ctx_, t), "set_exact_pressure"); }
+
+  // The two halves of the step around the Poisson solve:
+  // calculate_velocity_divergence (include/VelocityDivergence.h:9-20) into
+  // the pressure buffer, and update_pressure + update_velocity_pressure_gradient
+  // (src/Timestep.cpp:66-81).
+  void calculate_velocity_divergence(int velocity_set, double dt) {
+    check(mifgpu_divergence(ctx_, velocity_set, dt), "divergence");
+  }
+  void update_pressure_and_velocity(int velocity_set, double dt) {
+    check(mifgpu_project(ctx_, velocity_set, dt), "project");
+  }
+
+  // writeVTK, writeDat, writeVTKFullMesh (include/VTKDatExport.h:10-29) from
+  // the device-resident fields; the same bytes as the reference's writers.
+  void writeVTK(const std::string &filename) { check(mifgpu_write_vtk(ctx_, filename.c_str()), "write_vtk"); }
+  void writeDat(const std::string &filename, int direction, double x, double y, double z) {
+    check(mifgpu_write_dat(ctx_, filename.c_str(), direction, x, y, z), "write_dat");
+  }
+  void writeVTKFullMesh(const std::string &filename) {
+    check(mifgpu_write_vtk_full_mesh(ctx_, filename.c_str()), "write_vtk_full_mesh");
+  }
+
+  // Stream control: `stream` is a cudaStream_t (nullptr: the context's own).
+  void set_stream(void *stream) { check(mifgpu_set_stream(ctx_, stream), "set_stream"); }
+  void synchronize() { check(mifgpu_synchronize(ctx_), "synchronize"); }
+
+  // Reverse mode (no counterpart in the reference): see include/mifgpu.h.
+  // Each returns d loss / d forcing_amplitude (0 unless the forcing is
+  // MIFGPU_FORCING_TAYLOR_GREEN); ms, when non-null, receives the
+  // milliseconds of the forward pass, the segment recomputes and the reverse
+  // sweeps.
+  double gradient_ke(double t0, int nsteps, int checkpoint_every, const std::array<double, 6> &box, double *loss,
+                     std::array<double, 3> *ms = nullptr) {
+    double dalpha = 0.0;
+    std::array<double, 3> t{};
+    check(mifgpu_gradient_ke(ctx_, t0, nsteps, checkpoint_every, box.data(), loss, &dalpha, t.data()),
+          "gradient_ke");
+    if (ms) *ms = t;
+    return dalpha;
+  }
+  double backward(double t0, int nsteps, int checkpoint_every, const double *seed_u, const double *seed_v,
+                  const double *seed_w, const double *seed_p, std::array<double, 3> *ms = nullptr) {
+    double dalpha = 0.0;
+    std::array<double, 3> t{};
+    check(mifgpu_backward(ctx_, t0, nsteps, checkpoint_every, seed_u, seed_v, seed_w, seed_p, &dalpha, t.data()),
+          "backward");
+    if (ms) *ms = t;
+    return dalpha;
+  }
+  void download_adjoint(Field f, double *host) { check(mifgpu_download_adjoint(ctx_, f, host), "download_adjoint"); }
+  void set_forcing_amplitude(double alpha) {
+    check(mifgpu_set_forcing_amplitude(ctx_, alpha), "set_forcing_amplitude");
+  }
+
+  // Velocity error norms (L1, L2, Linf) that allocate nothing.
+  std::array<double, 3> velocity_error_norms_noalloc(double t) {
+    std::array<double, 3> out{};
+    check(mifgpu_velocity_error_norms_noalloc(ctx_, t, out.data()), "velocity_error_norms_noalloc");
+    return out;
+  }
+
+  // Instrumentation (no counterpart in the reference).
+  std::array<double, MIFGPU_PROF_CLASSES> profile_step(double t_n, int reps) {
+    std::array<double, MIFGPU_PROF_CLASSES> ms{};
+    check(mifgpu_profile_step(ctx_, t_n, reps, ms.data()), "profile_step");
+    return ms;
+  }
+  long long launch_count() const {
+    long long n = 0;
+    check(mifgpu_launch_count(ctx_, &n), "launch_count");
+    return n;
+  }
+  size_t device_bytes() const {
+    size_t n = 0;
+    check(mifgpu_device_bytes(ctx_, &n), "device_bytes");
+    return n;
+  }
+  // The current device's FP64 FMA rate in TFLOP/s; needs no context.
+  static double probe_fp64_fma() {
+    double tflops = 0.0;
+    const int rc = mifgpu_probe_fp64_fma(&tflops);
+    if (rc != MIFGPU_OK) throw Error(rc, "probe_fp64_fma failed");
+    return tflops;
+  }
+
   mifgpu_ctx *handle() { return ctx_; }
 
  private:

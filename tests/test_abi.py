@@ -20,6 +20,24 @@ def test_header_declares_the_binding_list(mifgpu_lib):
     assert declared_functions() == sorted(set(mifgpu_lib.EXPORTED))
 
 
+def test_cpp_mirror_wraps_every_declared_function():
+    hpp = open(os.path.join(REPO, "include", "mifgpu.hpp")).read()
+    assert [f for f in declared_functions() if f not in hpp] == []
+
+
+def test_cpp_mirror_compiles_and_links_against_the_library(tmp_path, mifgpu_lib):
+    """Every mirror method is called once (tests/cpp/mirror_api_check.cpp);
+    the program is compiled, linked with no undefined symbol, and not run."""
+    import subprocess
+
+    src = os.path.join(REPO, "tests", "cpp", "mirror_api_check.cpp")
+    pkg = os.path.dirname(mifgpu_lib.__file__)
+    out = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(REPO, "include"), "-o",
+                          str(tmp_path / "mirror_api_check"), src, "-L", pkg, "-lmifgpu", "-Wl,--no-undefined"],
+                         capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+
+
 def test_library_exports_every_declared_symbol(mifgpu_lib):
     lib = mifgpu_lib.load_library()
     for name in declared_functions():
