@@ -5,15 +5,21 @@ the Ethier-Steinman exact Navier-Stokes solution, on the unit cube at 512^3
 cells (513^3 nodes, every face Dirichlet with the exact velocity,
 homogeneous-Neumann DCT-I Poisson), Re = 1000, dt = 1e-4 (64/512)^2 (dt
 scaled with h^2 as in the large manufactured runs), no forcing (mif::timestep
-unchanged), mixed precision (f32 storage and stencils, f64 eigenvalue
-division). Inputs are the analytic fields at t = 0, generated on the device
-(synthetic; no dataset). The L-infinity velocity error against the exact
-solution after the run is reported for the mixed run and for the FP64 run of
-the same workload (the matched-error comparison).
+unchanged). Inputs are the analytic fields at t = 0, generated on the device
+(synthetic; no dataset).
+
+Precision of the headline (--precision compensated, the default): float
+fields, stencils and transforms, with the velocity state compensated by a
+bfloat16 residual per component (MIFGPU_MIXED_COMPENSATED); the eigenvalues
+and 1/(lx+ly+lz) are computed in double and applied as a float table; mean
+removal and norms in double. The same workload then runs in FP64 and in the
+plain float mode over the same window: `matched_error` gives the headline's
+L-infinity velocity error against the exact solution over FP64's (the
+"matched L-inf error" condition, target <= 2) and the speed-up over FP64.
 
 Extra modes (each prints one JSON line): --configs runs the reference's
 benchmark configurations 1-3 at their sizes; --sweep runs the Ethier-Steinman
-refinement 32^3 -> 768^3 in FP64 and mixed precision (convergence order and
+refinement 32^3 -> 768^3 in FP64 and both float modes (convergence order and
 matched error); --adjoint-only runs the adjoint workload alone.
 
 Arms:
@@ -24,9 +30,9 @@ Arms:
                     D2H inside the timed region); `roofline` of the dominant
                     kernel class; `cpu_baseline` of the oracle on a bounded sample.
   --impl reference  the reference's CPU algorithm (the bit-exact C restatement
-                    under oracle/, since the reference library itself cannot be
-                    rebuilt without its sources) on every host core, one
-                    independent replica per core, on a bounded sample.
+                    under oracle/, built with the reference's optimisation
+                    flags) on every host core, one independent replica per
+                    core, on a bounded 128^3 sample of the same workload.
 Multi-GPU: the path does not shard; N ranks run N independent replicas
 (weak scaling, no collective on the data path).
 """
@@ -73,24 +79,48 @@ WORKLOADS = {
                        1e-4 * (64.0 / 512.0) ** 2, 1, 2),
 }
 
+PRECISIONS = {"fp64": 0, "mixed": 1, "compensated": 2}
+
 # Algorithmic HBM sweeps (full-field reads + writes) per launch of each kernel
-# class; times the field bytes and the cell count give algorithmic bytes.
+# class, in units of one field of the working type (4 B in the float modes,
+# 8 B in FP64); times the unit and the cell count give algorithmic bytes.
 SWEEPS = {"stage": 11.0, "divergence": 4.0, "x_forward": 2.0, "y_forward": 2.0, "z_fused": 2.0,
           "y_inverse": 2.0, "x_inverse": 2.0, "project": 9.0}
+# The compensated state adds its bfloat16 residuals (2 B, half a float sweep
+# each): the stages and projections read and write three, the divergence
+# reads three.
+COMPENSATED_EXTRA = {"stage": 3.0, "divergence": 1.5, "project": 3.0}
 LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3, "z_fused": 3, "y_inverse": 3,
                      "x_inverse": 3, "project": 3}
+
+
+def sweeps(precision: str) -> dict:
+    out = dict(SWEEPS)
+    if precision == "compensated":
+        for k, v in COMPENSATED_EXTRA.items():
+            out[k] += v
+    return out
+
+
+def step_sweeps(precision: str) -> float:
+    """Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps +
+    9 projection) = 102; the compensated state adds 3 x (3 + 1.5 + 3) = 22.5."""
+    return sum(v * LAUNCHES_PER_STEP[k] for k, v in sweeps(precision).items())
+
+
 # DRAM read + write bytes over algorithmic bytes, from ncu captures of the
 # stage kernels on the 256x256x512 profiling case and of the line sweeps on
 # the 512x256x256 one: applied to the full launch. (The fused z sweep's
 # figure includes its 1/lambda table, one more field-sized read.)
-MEASURED_TRAFFIC_RATIO = {"stage": 1.06, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
-                          "x_inverse": 0.82}
+MEASURED_TRAFFIC_RATIO = {
+    "mixed": {"stage": 1.06, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
+              "x_inverse": 0.82},
+    "compensated": {"x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81, "x_inverse": 0.82},
+}
 # FP64 operations of one FP64 step per cell (an FMA counted as two), from the
 # DFMA / DADD / DMUL instruction counters of an ncu capture of the
 # 256x256x512 case; the 512^3 step's longer x and y transforms add a few per cent.
 FP64_FLOPS_PER_CELL_STEP = 1249.0
-# Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps + 9 projection).
-STEP_SWEEPS = 102.0
 # The same step with the divergence fused into the x-forward sweep and the
 # projection into the x-inverse sweep (the fused dataflow): 90 sweeps.
 FUSED_STEP_SWEEPS = 90.0
@@ -224,33 +254,55 @@ def replica_throughput(ms_local: float, world: int, cells: int, steps: int) -> t
 
 # ---------------------------------------------------------------- CPU baseline
 
+CPU_FLAGS = "-Ofast -funroll-all-loops -flto (the reference's Makefile:26 flags without -march=native)"
+
+
+def cpu_model() -> str:
+    try:
+        import platform
+
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part")):
+                    return f"{platform.machine()} {ln.split(':', 1)[1].strip()}"
+        return platform.machine()
+    except Exception:
+        return "unknown"
+
+
 def _cpu_worker(args):
-    n, steps, periodic, size, Re, dt, kind, forcing = args
+    """One replica of the CPU step: `warmup` untimed steps, then `steps`
+    timed ones; returns (cells per step, [seconds per timed step])."""
+    n, warmup, steps, periodic, size, Re, dt, kind, forcing = args
     import oracle as O
 
     case = O.Case(n_global=(n, n, n), size=size, Re=Re, dt=dt, periodic=periodic, exact_kind=kind, forcing=forcing)
-    s = O.OracleSolver(case)
+    s = O.OracleFastSolver(case)
     s.set_exact_velocity(0, 0.0, True)
     s.set_exact_pressure(0.0)
-    s.timestep(0.0)  # warm-up
-    t0 = time.perf_counter()
+    for k in range(warmup):
+        s.timestep(k * dt)
+    times = []
     for k in range(steps):
-        s.timestep((k + 1) * dt)
-    el = time.perf_counter() - t0
-    return case.cells() * steps, el
+        t0 = time.perf_counter()
+        s.timestep((warmup + k) * dt)
+        times.append(time.perf_counter() - t0)
+    return case.cells(), times
 
 
-def cpu_baseline(workers: int, n: int = 97, steps: int = 3):
-    """The oracle (bit-exact restatement of the reference's step) on a bounded
-    sample of the same workload family: an n^3-node manufactured cube,
-    `steps` timed steps per worker, one worker per core."""
+def cpu_run(workers: int, n: int, warmup: int, steps: int, workload: str = "cube512"):
+    """The reference's step (the oracle's C restatement in its timing build,
+    oracle/libmif_oracle_fast.so) on `workers` independent replicas, one per
+    core, each an n^3-node sample of the workload family. Returns per timed
+    step the whole-job Gcell-steps/s (all replicas' cells over the slowest
+    replica's time) and the wall time."""
     import multiprocessing as mp
 
     import oracle as O
 
-    O.build(with_ref=False)
-    w = WORKLOADS["cube512"]
-    job = (n, steps, w[3], w[1], w[4], w[5], w[6], w[7])
+    O.build(with_ref=False, fast=True)
+    w = WORKLOADS[workload]
+    job = (n, warmup, steps, w[3], w[1], w[4], w[5], w[6], w[7])
     t0 = time.perf_counter()
     if workers == 1:
         res = [_cpu_worker(job)]
@@ -260,11 +312,18 @@ def cpu_baseline(workers: int, n: int = 97, steps: int = 3):
             res = pool.map(_cpu_worker, [job] * workers)
     wall = time.perf_counter() - t0
     cells = sum(r[0] for r in res)
-    per_worker = max(r[1] for r in res)
-    return {"value": cells / per_worker / 1e9, "unit": UNIT, "cores": workers, "kind": "port",
-            "sample": f"{n - 1}^3-cell Ethier-Steinman cube (the default workload at a smaller size), {steps} steps "
-                      f"per core after "
-                      f"1 warm-up, {workers} independent replicas, oracle/mif_oracle.c built -O2 "
+    per_step = [cells / max(r[1][k] for r in res) / 1e9 for k in range(steps)]
+    return per_step, wall
+
+
+def cpu_baseline(workers: int = 1, n: int = 129, steps: int = 2):
+    """The bounded CPU sample beside the GPU number: one core, a 128^3-cell
+    Ethier-Steinman cube (the default workload at a smaller size)."""
+    per_step, wall = cpu_run(workers, n, 1, steps)
+    return {"value": statistics.median(per_step), "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{n - 1}^3-cell Ethier-Steinman cube (the default workload at a smaller size), {steps} timed "
+                      f"steps after 1 warm-up, {workers} replica(s); oracle/mif_oracle.c (bit-exact restatement "
+                      f"of the reference's step, FFT stand-in for FFTW) built {CPU_FLAGS}; {cpu_model()} "
                       f"(wall {wall:.1f}s)"}
 
 
@@ -480,6 +539,20 @@ def timed_run(s, stream, t0, nsteps):
     return e0.elapsed_time(e1) / nsteps
 
 
+def float_vs_fp64(c):
+    """Each float mode's final velocity against the FP64 run's (L-infinity over
+    max|u|) and its speed-up; drops the fields."""
+    import numpy as np
+
+    umax = max(float(np.abs(c["fp64"]["final"][nm]).max()) for nm in "uvw")
+    for pname in ("mixed", "compensated"):
+        c[pname + "_vs_fp64_velocity_linf"] = max(
+            float(np.abs(c[pname]["final"][nm] - c["fp64"]["final"][nm]).max()) for nm in "uvw") / umax
+        c[pname + "_speedup"] = round(c["fp64"]["ms_per_step"] / c[pname]["ms_per_step"], 2)
+    for pname in ("fp64", "mixed", "compensated"):
+        del c[pname]["final"]
+
+
 def config_suite(stream):
     """The reference's benchmark configurations 1-3 at their sizes, FP64 and
     mixed: Gcell-steps/s, errors against the analytic solution (config 1) or
@@ -500,7 +573,7 @@ def config_suite(stream):
 
     # 1: 64^3 manufactured cube, SINCOS + forcing, FP64, 10 steps of 1e-4
     c1 = {}
-    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED), ("compensated", mifgpu.MIXED_COMPENSATED)):
         s = make((65,) * 3, (1.0,) * 3, (0.0,) * 3, (False,) * 3, 1000.0, 1e-4, prec, 1, 2)
         s.set_exact_velocity(0, 0.0)
         s.set_exact_pressure(0.0)
@@ -520,7 +593,7 @@ def config_suite(stream):
     size = (2 * pi,) * 3
     fields = {}
     c2 = {}
-    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED), ("compensated", mifgpu.MIXED_COMPENSATED)):
         s = make(n_g, size, (0.0,) * 3, (True,) * 3, 1600.0, 2e-3, prec, 0, 0)
         if not fields:
             noise = solenoidal_noise(s.shape, (256,) * 3, size, (-1,) * 3, 16, 1e-2, 11)
@@ -538,12 +611,7 @@ def config_suite(stream):
                      "final": {nm: s.download(nm) for nm in "uvw"}}
         s.close()
         torch.cuda.empty_cache()
-    umax = max(float(np.abs(c2["fp64"]["final"][nm]).max()) for nm in "uvw")
-    c2["mixed_vs_fp64_velocity_linf"] = max(
-        float(np.abs(c2["mixed"]["final"][nm] - c2["fp64"]["final"][nm]).max()) for nm in "uvw") / umax
-    for pname in ("fp64", "mixed"):
-        del c2[pname]["final"]
-    c2["mixed_speedup"] = round(c2["fp64"]["ms_per_step"] / c2["mixed"]["ms_per_step"], 2)
+    float_vs_fp64(c2)
     out["2_tgv256_periodic"] = c2
 
     # 3: channel [0,4pi]x[0,2]x[0,2pi], 512x256x512, periodic x z, walls in y, Re 5000, dt 5e-4, 50 steps
@@ -552,7 +620,7 @@ def config_suite(stream):
     per = (True, False, True)
     fields = {}
     c3 = {}
-    for pname, prec in (("mixed", mifgpu.MIXED), ("fp64", mifgpu.FP64)):
+    for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED), ("compensated", mifgpu.MIXED_COMPENSATED)):
         s = make(n_g, size, (0.0,) * 3, per, 5000.0, 5e-4, prec, 0, 0)
         if not fields:
             noise = solenoidal_noise(s.shape, (512, 256, 512), size, (-1, 0, -1), 16, 1e-2, 12)
@@ -569,20 +637,17 @@ def config_suite(stream):
                      "final": {nm: s.download(nm) for nm in "uvw"}}
         s.close()
         torch.cuda.empty_cache()
-    umax = max(float(np.abs(c3["fp64"]["final"][nm]).max()) for nm in "uvw")
-    c3["mixed_vs_fp64_velocity_linf"] = max(
-        float(np.abs(c3["mixed"]["final"][nm] - c3["fp64"]["final"][nm]).max()) for nm in "uvw") / umax
-    for pname in ("fp64", "mixed"):
-        del c3[pname]["final"]
-    c3["mixed_speedup"] = round(c3["fp64"]["ms_per_step"] / c3["mixed"]["ms_per_step"], 2)
+    float_vs_fp64(c3)
     out["3_channel512x256x512"] = c3
     return out
 
 
 def sweep(stream, sizes=(32, 64, 128, 256, 512, 768)):
     """Ethier-Steinman refinement (the reference's full-step test case on the
-    unit cube): 2 steps of dt = 5e-5 from t = 0, FP64 and mixed, L-infinity
-    velocity and pressure errors against the exact solution, observed orders."""
+    unit cube): 2 steps of dt = 5e-5 from t = 0 (one time window for every
+    size, so the observed order is the spatial one), FP64, mixed and
+    compensated, L-infinity velocity and pressure errors against the exact
+    solution, observed orders."""
     import torch
 
     import mifgpu
@@ -591,7 +656,7 @@ def sweep(stream, sizes=(32, 64, 128, 256, 512, 768)):
     rows = []
     for n in sizes:
         row = {"cells": n}
-        for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+        for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED), ("compensated", mifgpu.MIXED_COMPENSATED)):
             s = mifgpu.Solver(n_global=(n + 1,) * 3, Re=1000.0, dt=T / nt, precision=prec,
                               boundary_kind=mifgpu.FIELD_ETHIER)
             s.set_stream(stream.cuda_stream)
@@ -606,12 +671,13 @@ def sweep(stream, sizes=(32, 64, 128, 256, 512, 768)):
             row[pname] = {"velocity_linf": nrm[2], "pressure_linf": nrm[5], "ms_per_step": round(ms, 4)}
             s.close()
             torch.cuda.empty_cache()
-        row["mixed_over_fp64_velocity_linf"] = row["mixed"]["velocity_linf"] / row["fp64"]["velocity_linf"]
+        for pname in ("mixed", "compensated"):
+            row[pname + "_over_fp64_velocity_linf"] = row[pname]["velocity_linf"] / row["fp64"]["velocity_linf"]
         rows.append(row)
     import math
 
     for a, b in zip(rows, rows[1:]):
-        for pname in ("fp64", "mixed"):
+        for pname in ("fp64", "mixed", "compensated"):
             b[pname]["velocity_order"] = math.log(a[pname]["velocity_linf"] / b[pname]["velocity_linf"]) / \
                 math.log(b["cells"] / a["cells"])
             b[pname]["pressure_order"] = math.log(a[pname]["pressure_linf"] / b[pname]["pressure_linf"]) / \
@@ -620,6 +686,62 @@ def sweep(stream, sizes=(32, 64, 128, 256, 512, 768)):
 
 
 # ------------------------------------------------------------------ GPU arm
+
+def workload_cells(workload: str) -> int:
+    cells = 1
+    for n in WORKLOADS[workload][0]:
+        cells *= n - 1
+    return cells
+
+
+def line_config(workload: str, precision: str, world: int) -> dict:
+    """The `config` of both arms' JSON lines (the same workload and settings)."""
+    n_global, size, origin, periodic, Re, dt, kind, forcing = WORKLOADS[workload]
+    elem = 8 if precision == "fp64" else 4
+    field_gb = 11 * elem * workload_cells(workload) / 1e9
+    return {"workload": workload, "n_global": list(n_global), "cells": workload_cells(workload),
+            "precision": precision, "periodic": list(periodic), "Re": Re, "dt": dt,
+            "parallelism": f"replicas{world}",
+            "l2": "inputs larger than L2 (fields ~%.1f GB)" % field_gb}
+
+
+def make_solver(mifgpu, workload: str, precision: str, stream):
+    n_global, size, origin, periodic, Re, dt, kind, forcing = WORKLOADS[workload]
+    s = mifgpu.Solver(n_global=n_global, size=size, origin=origin, Re=Re, dt=dt, periodic=periodic,
+                      precision=PRECISIONS[precision], boundary_kind=kind, forcing=forcing)
+    s.set_stream(stream.cuda_stream)
+    s.set_exact_velocity(0, 0.0)
+    s.set_exact_pressure(0.0)
+    return s
+
+
+def comparison_run(mifgpu, workload: str, precision: str, stream, n_timed: int, total_steps: int) -> dict:
+    """Another precision on the same workload: `n_timed` graph-replayed steps
+    timed with CUDA events, and the velocity error against the exact solution
+    after `total_steps` steps (the headline run's window)."""
+    import torch
+
+    dt = WORKLOADS[workload][5]
+    kind = WORKLOADS[workload][6]
+    cells = workload_cells(workload)
+    s = make_solver(mifgpu, workload, precision, stream)
+    s.run(0.0, 1)  # graph capture
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    s.run(dt, n_timed)
+    a1.record(stream)
+    torch.cuda.synchronize()
+    ms = a0.elapsed_time(a1) / n_timed
+    out = {"ms_per_step": round(ms, 4), "value": cells / (ms / 1e3) / 1e9}
+    s.run((1 + n_timed) * dt, max(0, total_steps - 1 - n_timed))
+    if kind != 0:
+        out["velocity_linf"] = s.error_norms(total_steps * dt)[2]
+        out["t"] = total_steps * dt
+    s.close()
+    torch.cuda.empty_cache()
+    return out
+
 
 def run_gpu(args):
     import torch
@@ -632,18 +754,12 @@ def run_gpu(args):
 
     pkg_build.build()
     n_global, size, origin, periodic, Re, dt, kind, forcing = WORKLOADS[args.workload]
-    prec = mifgpu.MIXED if args.precision == "mixed" else mifgpu.FP64
-    s = mifgpu.Solver(n_global=n_global, size=size, origin=origin, Re=Re, dt=dt, periodic=periodic,
-                      precision=prec, boundary_kind=kind, forcing=forcing)
+    prec = args.precision
     stream = torch.cuda.Stream()
-    s.set_stream(stream.cuda_stream)
-    s.set_exact_velocity(0, 0.0)
-    s.set_exact_pressure(0.0)
+    s = make_solver(mifgpu, args.workload, prec, stream)
     s.synchronize()
-    cells = 1
-    for n, p in zip(n_global, periodic):
-        cells *= (n - 1)
-    elem = 4 if prec == mifgpu.MIXED else 8
+    cells = workload_cells(args.workload)
+    elem = 8 if prec == "fp64" else 4
 
     # warm-up (graph capture happens here)
     t = 0.0
@@ -664,6 +780,7 @@ def run_gpu(args):
     t += args.steps * dt
     value, ms = replica_throughput(e0.elapsed_time(e1), world, cells, args.steps)
     launches = s.launch_count() - launches0
+    total_steps = args.warmup + args.steps
 
     # error against the analytic solution after the run (matched-error report)
     linf = None
@@ -675,21 +792,27 @@ def run_gpu(args):
     prof = s.profile_step(t, reps=2)
     t += 2 * dt
     peak, peak_kind = measured_peaks()
-    classes = {k: v for k, v in prof.items() if k in SWEEPS}
+    sw = sweeps(prec)
+    classes = {k: v for k, v in prof.items() if k in sw}
     dom = max(classes, key=lambda k: classes[k])
-    alg_bytes_launch = SWEEPS[dom] * elem * cells
+    alg_bytes_launch = sw[dom] * elem * cells
     avg_launch_ms = classes[dom] / LAUNCHES_PER_STEP[dom]
     achieved = alg_bytes_launch / (avg_launch_ms / 1e3) / 1e9
     # DRAM traffic per launch from one ncu capture of the same kernels on a
     # profiling case: measured read+write bytes over algorithmic bytes,
     # applied to this launch.
-    ratio = MEASURED_TRAFFIC_RATIO.get(dom) if args.precision == "mixed" else None
+    ratio = MEASURED_TRAFFIC_RATIO.get(prec, {}).get(dom)
     traffic = round(ratio * alg_bytes_launch) if ratio else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": round(avg_launch_ms, 4)}
     step_ms = ms / args.steps
-    step_roofline = STEP_SWEEPS * elem * cells / (step_ms / 1e3) / 1e9
+    ssw = step_sweeps(prec)
+    step_roofline = ssw * elem * cells / (step_ms / 1e3) / 1e9
+    per_kernel = {k: {"ms_per_step": round(v, 4),
+                      "gbs": round(sw[k] * LAUNCHES_PER_STEP[k] * elem * cells / (v / 1e3) / 1e9, 1),
+                      "frac": round(sw[k] * LAUNCHES_PER_STEP[k] * elem * cells / (v / 1e3) / 1e9 / peak, 4)}
+                  for k, v in classes.items() if v > 0}
 
     # end to end through the drop-in host call, pinned host buffers
     e2e = None
@@ -700,7 +823,6 @@ def run_gpu(args):
         for nm in names:
             host[nm].numpy()[...] = s.download(nm)
         bi = sum(h.numel() * 8 for h in host.values())
-        import numpy as np
 
         arrs = [host[nm].numpy() for nm in names]
         for _ in range(2):  # warm
@@ -745,50 +867,40 @@ def run_gpu(args):
         ceiling_s = step_ms / 1e3 + bi / (rates["h2d"] * 1e9) + bi / (rates["d2h"] * 1e9)
         e2e["link_gbs"] = {k: round(v, 1) for k, v in rates.items()}
         e2e["link_bound_value"] = round(world * cells / ceiling_s / 1e9, 4)
-        del np
+    s.close()
+    torch.cuda.empty_cache()
 
-    # FP64 comparison point on the same workload (fewer steps; FP64 is ALU-bound on GB300)
+    # the other precisions on the same workload and window
     fp64 = None
-    if prec == mifgpu.MIXED and not args.no_fp64:
-        s.close()
-        torch.cuda.empty_cache()
-        s64 = mifgpu.Solver(n_global=n_global, size=size, origin=origin, Re=Re, dt=dt, periodic=periodic,
-                            precision=mifgpu.FP64, boundary_kind=kind, forcing=forcing)
-        s64.set_stream(stream.cuda_stream)
-        s64.set_exact_velocity(0, 0.0)
-        s64.set_exact_pressure(0.0)
-        n64 = max(1, min(args.steps, 3))
-        s64.run(0.0, 1)
-        torch.cuda.synchronize()
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        s64.run(dt, n64)
-        a1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = a0.elapsed_time(a1) / n64
-        fp64 = {"ms_per_step": round(ms64, 3), "value": cells / (ms64 / 1e3) / 1e9,
-                "mixed_speedup": round(ms64 / step_ms, 2)}
+    if prec != "fp64" and not args.no_fp64:
+        fp64 = comparison_run(mifgpu, args.workload, "fp64", stream, max(1, min(args.steps, 3)), total_steps)
+        fp64["speedup_of_headline"] = round(fp64["ms_per_step"] / step_ms, 2)
         # both rooflines of the FP64 step: the FP64 pipe (its FMA rate probed
         # live) and HBM (the as-built sweeps at 8 bytes)
+        ms64 = fp64["ms_per_step"]
         peak64 = mifgpu.probe_fp64_fma()
         flops = FP64_FLOPS_PER_CELL_STEP * cells / (ms64 / 1e3) / 1e12
         fp64["fp64_alu_roofline"] = {"achieved_tflops": round(flops, 4), "peak_tflops": round(peak64, 4),
                                      "frac": round(flops / peak64, 4),
                                      "flops_per_cell_step": FP64_FLOPS_PER_CELL_STEP,
                                      "peak_source": "FMA-chain probe (mifgpu_probe_fp64_fma)"}
-        fp64["hbm_roofline"] = {"achieved_gbs": round(STEP_SWEEPS * 8 * cells / (ms64 / 1e3) / 1e9, 1),
-                                "peak_gbs": peak, "frac": round(STEP_SWEEPS * 8 * cells / (ms64 / 1e3) / 1e9 / peak, 4)}
-        s64.run((1 + n64) * dt, max(0, args.warmup + args.steps - 1 - n64))
-        if kind != 0:
-            t64 = (args.warmup + args.steps) * dt
-            fp64["velocity_linf"] = s64.error_norms(t64)[2]
-            fp64["t"] = t64
-        s64.close()
+        hbm64 = step_sweeps("fp64") * 8 * cells / (ms64 / 1e3) / 1e9
+        fp64["hbm_roofline"] = {"achieved_gbs": round(hbm64, 1), "peak_gbs": peak, "frac": round(hbm64 / peak, 4)}
+    mixed = None
+    if prec == "compensated" and not args.no_mixed:
+        mixed = comparison_run(mifgpu, args.workload, "mixed", stream, args.steps, total_steps)
+        mixed["note"] = "plain float state (stochastically rounded updates), no residual"
+    matched = None
+    if linf and fp64 and "velocity_linf" in fp64:
+        matched = {"velocity_linf": linf["velocity_linf"], "fp64_velocity_linf": fp64["velocity_linf"],
+                   "ratio": linf["velocity_linf"] / fp64["velocity_linf"], "target_ratio": 2.0,
+                   "speedup_vs_fp64": round(fp64["ms_per_step"] / step_ms, 2), "target_speedup": 1.7,
+                   "t": linf["t"]}
+        if mixed and "velocity_linf" in mixed:
+            matched["plain_mixed_ratio"] = mixed["velocity_linf"] / fp64["velocity_linf"]
 
     adjoint = None
     if not args.no_adjoint:
-        s.close()
-        torch.cuda.empty_cache()
         adjoint = adjoint_bench(stream)
 
     cpu = None
@@ -799,44 +911,42 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if prec == mifgpu.MIXED else "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "n_global": list(n_global), "cells": cells,
-                       "precision": args.precision, "periodic": list(periodic), "Re": Re, "dt": dt,
-                       "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (fields ~%.1f GB)" %
-                       (11 * elem * cells / 1e9)},
+            "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
+            "config": line_config(args.workload, prec, world),
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "step_roofline": {"bytes_per_cell_step": STEP_SWEEPS * elem, "achieved_gbs": round(step_roofline, 1),
-                              "frac": round(step_roofline / peak, 4),
-                              "fused_dataflow_bytes_per_cell_step": FUSED_STEP_SWEEPS * elem,
-                              "fused_dataflow_frac": round(step_roofline * FUSED_STEP_SWEEPS / STEP_SWEEPS / peak,
-                                                           4)},
-            "kernel_ms_per_step": {k: round(v, 4) for k, v in prof.items()},
-            "error": linf, "fp64": fp64, "adjoint": adjoint, "cpu_baseline": cpu,
+            "step_roofline": {"bytes_per_cell_step": ssw * elem, "achieved_gbs": round(step_roofline, 1),
+                              "frac": round(step_roofline / peak, 4)},
+            "kernel_ms_per_step": {k: round(v, 4) for k, v in prof.items()}, "kernels": per_kernel,
+            "error": linf, "matched_error": matched, "fp64": fp64, "mixed": mixed, "adjoint": adjoint,
+            "cpu_baseline": cpu,
         }
+        if prec == "mixed":
+            line["step_roofline"]["fused_dataflow_bytes_per_cell_step"] = FUSED_STEP_SWEEPS * elem
+            line["step_roofline"]["fused_dataflow_frac"] = round(step_roofline * FUSED_STEP_SWEEPS / ssw / peak, 4)
         print(json.dumps(line))
 
 
 def run_reference(args):
+    """The reference's CPU step on every host core (one replica per core, a
+    bounded 128^3 sample each), on this arm's metric, unit and config."""
     world, rank, local = dist_setup()
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    vals = []
-    for k in range(args.warmup + args.steps):
-        r = cpu_baseline(workers=cores, n=65, steps=1)
-        if k >= args.warmup:
-            vals.append(r["value"])
-    el = time.perf_counter() - t0
-    value = statistics.median(vals) if vals else 0.0
-    n_global = WORKLOADS[args.workload][0]
+    n = 129
+    per_step, wall = cpu_run(cores, n, args.warmup, args.steps, args.workload)
+    value = statistics.median(per_step) if per_step else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "n_global": list(n_global), "sample": "64^3 cells per core"},
+            "config": line_config(args.workload, args.precision, world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"64^3-cell Ethier-Steinman cube, 1 step per core per bench step, {cores} "
-                                       f"independent replicas (wall {el:.1f}s)"},
+                             "sample": f"{n - 1}^3-cell Ethier-Steinman cube per core (the workload's family at a "
+                                       f"smaller size), {args.warmup} warm-up + {args.steps} timed steps per "
+                                       f"replica, {cores} independent replicas, value the median over the timed "
+                                       f"steps of all replicas' cells over the slowest replica's time; "
+                                       f"oracle/mif_oracle.c (bit-exact restatement of the reference's step, FFT "
+                                       f"stand-in for FFTW) built {CPU_FLAGS}; {cpu_model()} (wall {wall:.1f}s)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -848,9 +958,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cube512", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="compensated", choices=sorted(PRECISIONS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--configs", action="store_true", help="the reference's configurations 1-3 (one JSON line)")

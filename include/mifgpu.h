@@ -34,12 +34,29 @@ extern "C" {
 #define MIFGPU_ECUDA (-2)    /* a CUDA call failed; see mifgpu_last_error */
 #define MIFGPU_ENOMEM (-3)   /* device allocation failed */
 #define MIFGPU_ENOTSUP (-4)  /* combination the reference does not define */
-#define MIFGPU_ENONFINITE (-5) /* the step produced NaN/Inf (watchdog) */
+#define MIFGPU_ENONFINITE (-5) /* a projection step produced NaN/Inf: the last
+                                  projection of every step checks each value
+                                  of phi, which a NaN/Inf anywhere in the
+                                  velocity reaches (mifgpu_timestep, _run,
+                                  _timestep_host, _timestep_nhn; the fields
+                                  hold the non-finite state) */
 
 enum mifgpu_precision {
   MIFGPU_FP64 = 0,  /* everything in double: the reference's USE_DOUBLE=1 build */
-  MIFGPU_MIXED = 1  /* fields and stencils in float; eigenvalue division,
-                       zero-mode handling and reductions in double */
+  MIFGPU_MIXED = 1, /* fields and stencils in float; the eigenvalues and
+                       1/(lx+ly+lz) computed in double and applied as a float
+                       table; zero-mode handling and reductions in double;
+                       the state updates round stochastically */
+  MIFGPU_MIXED_COMPENSATED = 2 /* as MIXED, and every velocity component of the
+                       state carries a bfloat16 residual: each state update
+                       (RK stage, projection, boundary fill) is an error-free
+                       float sum whose rounding error is kept in the residual,
+                       and the divergence reads hi + residual, so the state is
+                       held to about 32 significant bits while the stencils and
+                       transforms still read float. Host transfers of velocity
+                       set 0 and the error norms see hi + residual. The
+                       velocity-only step and the reverse mode return
+                       MIFGPU_ENOTSUP in this mode. */
 };
 
 /* Analytic field families used for Dirichlet boundary data, forcing and
@@ -50,8 +67,18 @@ enum mifgpu_field_kind {
   MIFGPU_FIELD_SINCOS = 1, /* u = sin x cos y sin z sin t, v = cos x sin y sin z sin t,
                               w = 2 cos x cos y cos z sin t, p = cos x cos y sin z sin t
                               (generators/manufsol_velocity.py:55-57) */
-  MIFGPU_FIELD_ETHIER = 2  /* exact NS solution of test/full_test.cpp
+  MIFGPU_FIELD_ETHIER = 2, /* exact NS solution of test/full_test.cpp
                               (generators/manufsol.py:35-72) */
+  MIFGPU_FIELD_CALLER = 3  /* any exact velocity: the caller supplies the
+                              Dirichlet face values of every stage
+                              (mifgpu_set_boundary_values) and, for the
+                              non-homogeneous Neumann step, the normal
+                              pressure-gradient data
+                              (mifgpu_set_pressure_gradient_faces). There is
+                              no analytic field: set_exact_*, adjust_pressure,
+                              the error norms and the reverse mode return
+                              MIFGPU_ENOTSUP, and mifgpu_run takes one step
+                              per call */
 };
 
 /* Forcing added to the momentum right-hand side of the projection step.
@@ -162,6 +189,40 @@ int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n);
  *   project        p += phi and set -= dt * grad(phi) on interior points
  *                  (src/Timestep.cpp:66-81) */
 int mifgpu_apply_bc(mifgpu_ctx *ctx, int set, double t);
+
+/* Caller boundary data for boundary_kind MIFGPU_FIELD_CALLER. Replaces the
+ * evaluation of the caller's exact_velocity inside the step
+ * (VelocityTensor::apply_bc, src/VelocityTensor.cpp:36-233, called by
+ * src/Timestep.cpp:110,120,130 with exact_velocity.set_time(t_k)). u, v, w are
+ * host arrays in the reference layout (extents of fields 0, 1, 2); only their
+ * Dirichlet face planes are read: the values apply_bc writes there at the
+ * slot's time (a caller gets them by running the reference's own apply_bc on
+ * a scratch VelocityTensor). Slot 0 is what mifgpu_apply_bc imposes; slots 1,
+ * 2, 3 are the stage times time_1, time_2, final_time of the next
+ * mifgpu_timestep / _timestep_host / _timestep_nhn / _run(ctx, t, 1) (and of
+ * mifgpu_timestep_velocity's stages). Copied at the call; a slot keeps its
+ * data until set again (all zero at first). */
+int mifgpu_set_boundary_values(mifgpu_ctx *ctx, int slot, const double *u, const double *v, const double *w);
+
+/* Caller data of the non-homogeneous Neumann step (MIFGPU_FIELD_CALLER):
+ * replaces exact_pressure_gradient.get_difference_over_time(t_k, t_{k-1}) of
+ * src/Timestep.cpp:85-90, i.e. grad p(t_{k-1}) - grad p(t_k), for stage k =
+ * slot (1..3; slot 0 is overwritten by mifgpu_solve_pressure_nhn). faces[f]
+ * holds the normal component on face f = x_min, x_max, y_min, y_max, z_min,
+ * z_max at the face's pressure nodes, the two other axes in order, lower one
+ * fastest: (j, k) -> j + Ny k on x faces, (i, k) -> i + Nx k on y faces,
+ * (i, j) -> i + Nx j on z faces (Nx, Ny: the pressure extents). Copied at the
+ * call. */
+int mifgpu_set_pressure_gradient_faces(mifgpu_ctx *ctx, int slot, const double *const faces[6]);
+
+/* solve_pressure_equation_non_homogeneous_neumann (include/PressureEquation.h:15-19,
+ * src/PressureEquation.cpp:276-286): phi := div(set)/dt plus the boundary
+ * terms of apply_non_homogeneous_neumann (src/PressureEquation.cpp:10-56)
+ * from `faces` (the normal component of the caller's exact_pressure_gradient
+ * at the face nodes, laid out as for mifgpu_set_pressure_gradient_faces),
+ * then the spectral solve. Any boundary kind; every axis must be
+ * non-periodic (MIFGPU_ENOTSUP otherwise). */
+int mifgpu_solve_pressure_nhn(mifgpu_ctx *ctx, int set, double dt, const double *const faces[6]);
 int mifgpu_solve_pressure(mifgpu_ctx *ctx, int set, double dt);
 int mifgpu_divergence(mifgpu_ctx *ctx, int set, double dt);
 int mifgpu_project(mifgpu_ctx *ctx, int set, double dt);
@@ -264,11 +325,14 @@ int mifgpu_set_forcing_amplitude(mifgpu_ctx *ctx, double alpha);
  * totals); nothing in it has to start at zero, because every element the call
  * reads it has written before. The reduction runs in a fixed order, so the
  * result is bitwise reproducible. The call returns MIFGPU_EINVAL, with a
- * message, for a z extent above 4002 points (more than 4000 interior
- * planes), and when the context's device is not the current device. The
- * first call on a device looks up the array's address (cudaGetSymbolAddress)
- * and caches it; make that first call before any stream capture begins on
- * the device. The array is shared by every context on a device: calls whose
+ * message, for more than 4000 interior z planes, that is n_global[2] above
+ * 4002 on a Dirichlet z axis or above 4001 on a periodic one, and when the
+ * context's device is not the current device. The first call on a device
+ * (and the first after its context was re-created, e.g. by cudaDeviceReset)
+ * looks up the array's address (cudaGetSymbolAddress) and caches it; make
+ * that first call before any stream capture begins on the device. In the
+ * compensated precision the velocity is read as hi + residual, as in
+ * mifgpu_error_norms. The array is shared by every context on a device: calls whose
  * executions overlap (other threads, other streams or contexts on the same
  * device) race on it, so the caller serialises them. Returns after the three
  * numbers have reached `out`. */

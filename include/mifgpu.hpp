@@ -97,6 +97,23 @@ class Solver {
     check(mifgpu_solve_pressure(ctx_, velocity_set, dt), "solve_pressure");
   }
   void apply_bc(int velocity_set, double t) { check(mifgpu_apply_bc(ctx_, velocity_set, t), "apply_bc"); }
+
+  // Caller boundary data (boundary_kind MIFGPU_FIELD_CALLER): the Dirichlet
+  // face planes of u, v, w for time slot `slot` (0: apply_bc; 1..3: the
+  // stages of the next step), and the normal pressure-gradient faces of the
+  // non-homogeneous Neumann step.
+  void set_boundary_values(int slot, const double *u, const double *v, const double *w) {
+    check(mifgpu_set_boundary_values(ctx_, slot, u, v, w), "set_boundary_values");
+  }
+  void set_pressure_gradient_faces(int slot, const std::array<const double *, 6> &faces) {
+    check(mifgpu_set_pressure_gradient_faces(ctx_, slot, faces.data()), "set_pressure_gradient_faces");
+  }
+  // solve_pressure_equation_non_homogeneous_neumann (include/PressureEquation.h:15-19)
+  // with the caller's normal pressure-gradient faces.
+  void solve_pressure_equation_non_homogeneous_neumann(int velocity_set, double dt,
+                                                       const std::array<const double *, 6> &faces) {
+    check(mifgpu_solve_pressure_nhn(ctx_, velocity_set, dt, faces.data()), "solve_pressure_nhn");
+  }
   void adjust_pressure(double t) { check(mifgpu_adjust_pressure(ctx_, t), "adjust_pressure"); }
   std::array<double, 9> error_norms(double t) {
     std::array<double, 9> out{};

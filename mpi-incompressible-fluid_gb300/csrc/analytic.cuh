@@ -14,7 +14,7 @@
 
 namespace mifgpu {
 
-enum { kFieldZero = 0, kFieldSincos = 1, kFieldEthier = 2 };
+enum { kFieldZero = 0, kFieldSincos = 1, kFieldEthier = 2, kFieldCaller = 3 };  // kFieldCaller: no analytic field
 
 template <typename TE>
 __device__ __forceinline__ TE an_sin(TE x);

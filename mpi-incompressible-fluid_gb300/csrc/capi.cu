@@ -60,6 +60,13 @@ struct ImplBase {
   virtual int download_adjoint(mifgpu_ctx *ctx, int id, double *host) = 0;
   virtual void drop_graphs() = 0;
   virtual int fetch_box(mifgpu_ctx *ctx, int id, const int lo[3], const int n[3], double *out) = 0;
+  // The compensated state's residuals (off unless MIFGPU_MIXED_COMPENSATED).
+  virtual Residual residual() const = 0;
+  // Caller boundary data (MIFGPU_FIELD_CALLER) and the stand-alone
+  // non-homogeneous Neumann solve.
+  virtual int set_boundary_values(mifgpu_ctx *ctx, int slot, const double *const vel[3]) = 0;
+  virtual int set_gradient_faces(mifgpu_ctx *ctx, int slot, const double *const faces[6]) = 0;
+  virtual int solve_pressure_nhn(mifgpu_ctx *ctx, int set, double dt) = 0;
 };
 
 }  // namespace
@@ -176,6 +183,7 @@ struct Impl final : ImplBase {
   double *slots = nullptr;  // device: kSlotSize doubles per step
   int slots_cap = 0;
   int *step_ctr = nullptr;  // device step index the graph reads and advances
+  int *nonfinite = nullptr; // device flag: a projection saw a NaN or Inf in phi
   double *acc = nullptr;    // device reduction scratch
   double *staging = nullptr;
   size_t staging_elems = 0;
@@ -189,8 +197,16 @@ struct Impl final : ImplBase {
   cudaStream_t copy_stream[kCopyStreams] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t xfer_ev[kXferSlots + 1][kCopyStreams] = {};
   T *grad_block = nullptr;  // three fields for the pressure-gradient norm
-  double *face_tab = nullptr;  // float path: the families' face data in double
+  // MIFGPU_MIXED_COMPENSATED: the bfloat16 residuals of the velocity state
+  // (one triple shared by the three sets, see Residual).
+  __nv_bfloat16 *res_block = nullptr;
+  Residual res{};
+  double *face_tab = nullptr;  // float path: the families' face data in double; or the caller's
   FaceTables ftabs{};
+  // Caller pressure-gradient face data (slots 0..3), allocated on first use.
+  double *grad_tab = nullptr;
+  GradFaces gfaces{};
+  std::vector<double> pack;  // host packing buffer of the caller data
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   long long graph_launches[3][2] = {{0, 0}, {0, 0}, {0, 0}};
@@ -228,10 +244,13 @@ struct Impl final : ImplBase {
     cudaFree(ftab);
     cudaFree(slots);
     cudaFree(step_ctr);
+    cudaFree(nonfinite);
     cudaFree(acc);
     cudaFree(staging);
     cudaFree(grad_block);
+    cudaFree(res_block);
     cudaFree(face_tab);
+    cudaFree(grad_tab);
     cudaFree(adj_block);
     cudaFree(ckpt_block);
     cudaFree(snap_block);
@@ -256,6 +275,13 @@ struct Impl final : ImplBase {
     CK(cudaMemset(block, 0, sizeof(T) * field_elems * kNumFields));
     for (int f = 0; f < kNumFields; ++f) phys.f[f] = block + f * field_elems;
     remap();
+    if (ctx->prm.precision == MIFGPU_MIXED_COMPENSATED) {
+      if (cudaMalloc(&res_block, sizeof(__nv_bfloat16) * field_elems * 3) != cudaSuccess)
+        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the residual fields failed");
+      total_bytes += sizeof(__nv_bfloat16) * field_elems * 3;
+      CK(cudaMemset(res_block, 0, sizeof(__nv_bfloat16) * field_elems * 3));
+      for (int c = 0; c < 3; ++c) res.c[c] = res_block + c * field_elems;
+    }
     std::string perr;
     const int rc = ps.init(g, perr);
     if (rc) return fail(ctx, rc == -2 ? MIFGPU_ECUDA : MIFGPU_ENOTSUP, perr);
@@ -274,6 +300,8 @@ struct Impl final : ImplBase {
     if (int rc = init_face_tables(ctx)) return rc;
     CK(cudaMalloc(&step_ctr, sizeof(int)));
     CK(cudaMemset(step_ctr, 0, sizeof(int)));
+    CK(cudaMalloc(&nonfinite, sizeof(int)));
+    CK(cudaMemset(nonfinite, 0, sizeof(int)));
     CK(cudaMalloc(&acc, sizeof(double) * 16));
     CK(alloc_slots());
     CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
@@ -286,6 +314,7 @@ struct Impl final : ImplBase {
   // evaluation of exp/sin/cos products cost several ulp of |u| per fill).
   int init_face_tables(mifgpu_ctx *ctx) {
     const int kind = ctx->prm.boundary_kind;
+    if (kind == MIFGPU_FIELD_CALLER) return init_caller_tables(ctx);
     if (!std::is_same<T, float>::value || kind == 0 || (g.periodic[0] && g.periodic[1] && g.periodic[2]))
       return MIFGPU_OK;
     long n = 0;
@@ -305,6 +334,102 @@ struct Impl final : ImplBase {
     ftabs.tab = face_tab;
     for (int fn = 0; fn < 2; ++fn) launch_face_tables(g, kind, fn, face_tab, ftabs, nullptr);
     CK(cudaDeviceSynchronize());
+    return MIFGPU_OK;
+  }
+
+  // MIFGPU_FIELD_CALLER: the velocity face tables of the four time slots
+  // (slot 0 for mifgpu_apply_bc, slots 1..3 for the stages of the next step),
+  // zero until the caller sets them, and the pressure-gradient faces.
+  int init_caller_tables(mifgpu_ctx *ctx) {
+    long n = 0;
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) {
+        if (g.periodic[d]) continue;
+        const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+        for (int sd = 0; sd < 2; ++sd) {
+          ftabs.off[0][c][d][sd] = n;
+          n += (long)g.ext(c, a) * g.ext(c, b);
+        }
+      }
+    const long total = std::max(1L, n) * kCallerSlots;
+    if (cudaMalloc(&face_tab, sizeof(double) * total) != cudaSuccess)
+      return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the caller boundary tables failed");
+    total_bytes += sizeof(double) * total;
+    CK(cudaMemset(face_tab, 0, sizeof(double) * total));
+    ftabs.tab = face_tab;
+    ftabs.slot_stride = std::max(1L, n);
+    return ensure_grad_faces(ctx);
+  }
+
+  static constexpr int kCallerSlots = 4;
+
+  int ensure_grad_faces(mifgpu_ctx *ctx) {
+    if (grad_tab) return MIFGPU_OK;
+    const long E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
+    const long sz[6] = {E1 * E2, E1 * E2, E0 * E2, E0 * E2, E0 * E1, E0 * E1};
+    long n = 0;
+    for (int f = 0; f < 6; ++f) {
+      gfaces.off[f] = n;
+      n += sz[f];
+    }
+    if (cudaMalloc(&grad_tab, sizeof(double) * n * kCallerSlots) != cudaSuccess)
+      return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the pressure-gradient face tables failed");
+    total_bytes += sizeof(double) * n * kCallerSlots;
+    CK(cudaMemset(grad_tab, 0, sizeof(double) * n * kCallerSlots));
+    gfaces.tab = grad_tab;
+    gfaces.slot_stride = n;
+    return MIFGPU_OK;
+  }
+
+  // The Dirichlet face planes of host arrays u, v, w (reference layout),
+  // packed into slot `slot` of the caller velocity tables.
+  int set_boundary_values(mifgpu_ctx *ctx, int slot, const double *const vel[3]) override {
+    if (ctx->prm.boundary_kind != MIFGPU_FIELD_CALLER)
+      return fail(ctx, MIFGPU_EINVAL, "set_boundary_values needs boundary_kind MIFGPU_FIELD_CALLER");
+    pack.assign((size_t)ftabs.slot_stride, 0.0);
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) {
+        if (g.periodic[d]) continue;
+        const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+        const long ex = g.ext(c, 0), ey = g.ext(c, 1);
+        for (int sd = 0; sd < 2; ++sd) {
+          double *dst = pack.data() + ftabs.off[0][c][d][sd];
+          const long na = g.ext(c, a), nb = g.ext(c, b);
+          for (long pb = 0; pb < nb; ++pb)
+            for (long pa = 0; pa < na; ++pa) {
+              long pt[3];
+              pt[a] = pa;
+              pt[b] = pb;
+              pt[d] = sd ? g.ext(c, d) - 1 : 0;
+              dst[pa + na * pb] = vel[c][pt[0] + ex * (pt[1] + ey * pt[2])];
+            }
+        }
+      }
+    // a pageable source: the call returns once the data is staged
+    CK(cudaMemcpyAsync(face_tab + (size_t)slot * ftabs.slot_stride, pack.data(), sizeof(double) * pack.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    return MIFGPU_OK;
+  }
+
+  int set_gradient_faces(mifgpu_ctx *ctx, int slot, const double *const faces[6]) override {
+    if (int rc = ensure_grad_faces(ctx)) return rc;
+    for (int f = 0; f < 6; ++f) {
+      const long n = (f < 5 ? gfaces.off[f + 1] : gfaces.slot_stride) - gfaces.off[f];
+      CK(cudaMemcpyAsync(grad_tab + (size_t)slot * gfaces.slot_stride + gfaces.off[f], faces[f],
+                         sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    // pageable sources: each call returns once its data is staged
+    return MIFGPU_OK;
+  }
+
+  // phi := div(set)/dt + the flux terms of the slot-0 gradient faces, solved
+  // (solve_pressure_equation_non_homogeneous_neumann).
+  int solve_pressure_nhn(mifgpu_ctx *ctx, int set, double dt) override {
+    T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
+    launch_divergence<T>(g, F.f[kPhi], vel, dt, ctx->stream, &ctx->launches, set_res(set));
+    launch_neumann_flux_data<T>(g, F.f[kPhi], gfaces, 0, ctx->stream, &ctx->launches);
+    ps.solve(F.f[kPhi], ctx->stream, &ctx->launches);
+    CK(cudaGetLastError());
     return MIFGPU_OK;
   }
 
@@ -332,6 +457,15 @@ struct Impl final : ImplBase {
   }
 
   void *field_ptr(int id) override { return F.f[id]; }
+
+  Residual residual() const override { return res; }
+
+  // The residual array of field id: the compensated state is velocity set 0
+  // between steps, so only its components carry one at the host boundary.
+  __nv_bfloat16 *field_res(int id) const { return (res.on() && id < 3) ? res.c[id] : nullptr; }
+
+  // The residuals a sub-step on velocity set `set` uses: set 0's (the state).
+  Residual set_res(int set) const { return set == 0 ? res : Residual{}; }
 
   int ensure_staging(mifgpu_ctx *ctx) {
     const size_t need = (size_t)g.Es[0] * g.Es[1] * g.Es[2];
@@ -399,7 +533,7 @@ struct Impl final : ImplBase {
         CK(cudaEventRecord(xfer_ev[q][cs], copy_stream[cs]));
         CK(cudaStreamWaitEvent(ctx->stream, xfer_ev[q][cs], 0));
       }
-      launch_scatter<T>(g, F.f[ids[q]], xfer[q], e[0], e[1], e[2], ctx->stream, &ctx->launches);
+      launch_scatter<T>(g, F.f[ids[q]], xfer[q], e[0], e[1], e[2], ctx->stream, &ctx->launches, field_res(ids[q]));
       CK(cudaGetLastError());
     }
     return MIFGPU_OK;
@@ -415,7 +549,7 @@ struct Impl final : ImplBase {
       int e[3];
       field_extent(g, ids[q], e);
       const size_t n = (size_t)e[0] * e[1] * e[2];
-      launch_gather<T>(g, xfer[q], F.f[ids[q]], e[0], e[1], e[2], ctx->stream, &ctx->launches);
+      launch_gather<T>(g, xfer[q], F.f[ids[q]], e[0], e[1], e[2], ctx->stream, &ctx->launches, field_res(ids[q]));
       CK(cudaGetLastError());
       CK(cudaEventRecord(xfer_ev[q][0], ctx->stream));
       for (int c = 0; c < kCopyStreams; ++c) CK(cudaStreamWaitEvent(copy_stream[c], xfer_ev[q][0], 0));
@@ -433,21 +567,24 @@ struct Impl final : ImplBase {
 
   int set_exact(mifgpu_ctx *ctx, int id, double t) override {
     const int comp = id < 9 ? id % 3 : 3;
-    launch_set_exact<T>(g, F.f[id], comp, ctx->prm.boundary_kind, t, ctx->stream, &ctx->launches);
+    launch_set_exact<T>(g, F.f[id], comp, ctx->prm.boundary_kind, t, ctx->stream, &ctx->launches, field_res(id));
     CK(cudaGetLastError());
     return MIFGPU_OK;
   }
 
   // phi := div(set)/dt (+ Neumann flux) [-> Poisson solve -> periodic refresh]
   void enqueue_pressure(mifgpu_ctx *ctx, cudaStream_t s, int set, double dt, bool nhn, int slot_new, int slot_old,
-                        bool solve, long long *cnt) {
+                        bool solve, long long *cnt, const Residual &r) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
     // The divergence is its own streaming kernel: fused into the x-forward
     // sweep (PoissonSolver::solve's `vel` argument) its loads ran at the line
     // kernel's low occupancy and the pair took 2.5x longer on GB300.
     mark(MIFGPU_PROF_DIVERGENCE, s);
-    launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt);
-    if (nhn) launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
+    launch_divergence<T>(g, F.f[kPhi], vel, dt, s, cnt, r);
+    if (nhn && ctx->prm.boundary_kind == MIFGPU_FIELD_CALLER)
+      launch_neumann_flux_data<T>(g, F.f[kPhi], gfaces, slot_new, s, cnt);
+    else if (nhn)
+      launch_neumann_flux<T>(g, F.f[kPhi], ctx->prm.boundary_kind, tref(), slot_new, slot_old, s, cnt);
     if (!solve) return;
     std::function<void(int)> mk;
     if (prof) mk = [&](int q) { mark(MIFGPU_PROF_X_FORWARD + q, s); };
@@ -456,16 +593,17 @@ struct Impl final : ImplBase {
     launch_periodic_scalar<T>(g, F.f[kPhi], s, cnt);
   }
 
-  void enqueue_bc(mifgpu_ctx *ctx, cudaStream_t s, int set, int t_slot, long long *cnt) {
+  void enqueue_bc(mifgpu_ctx *ctx, cudaStream_t s, int set, int t_slot, long long *cnt, const Residual &r) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
     mark(MIFGPU_PROF_BOUNDARY, s);
-    launch_apply_bc<T>(g, vel, ctx->prm.boundary_kind, 0, tref(), t_slot, ftabs, s, cnt);
+    launch_apply_bc<T>(g, vel, ctx->prm.boundary_kind, 0, tref(), t_slot, ftabs, s, cnt, r);
   }
 
-  void enqueue_project(cudaStream_t s, int set, double dt, unsigned tag, long long *cnt) {
+  void enqueue_project(cudaStream_t s, int set, double dt, unsigned tag, long long *cnt, const Residual &r,
+                       int *watch = nullptr) {
     T *vel[3] = {F.vel(set, 0), F.vel(set, 1), F.vel(set, 2)};
     mark(MIFGPU_PROF_PROJECT, s);
-    launch_project<T>(g, F.f[kP], F.f[kPhi], vel, dt, tref(), tag, s, cnt);
+    launch_project<T>(g, F.f[kP], F.f[kPhi], vel, dt, tref(), tag, s, cnt, r, watch);
   }
 
   // The kernels of one step of the given variant, in stream order.
@@ -475,14 +613,15 @@ struct Impl final : ImplBase {
     const int kind = ctx->prm.boundary_kind;
     if (variant == kVariantVelocity) {
       StageScalars<T> sc{dt, 4, 1, 0.0};
+      const Residual none{};
       launch_stage<T>(g, F, kVelY2, sc, ft, kind, tref(), s, cnt);
-      enqueue_bc(ctx, s, 1, 1, cnt);
+      enqueue_bc(ctx, s, 1, 1, cnt, none);
       sc.sin_slot = 6;
       launch_stage<T>(g, F, kVelY3, sc, ft, kind, tref(), s, cnt);
-      enqueue_bc(ctx, s, 0, 2, cnt);
+      enqueue_bc(ctx, s, 0, 2, cnt, none);
       sc.sin_slot = 8;
       launch_stage<T>(g, F, kVelUStar, sc, ft, kind, tref(), s, cnt);
-      enqueue_bc(ctx, s, 1, 3, cnt);
+      enqueue_bc(ctx, s, 1, 3, cnt, none);
       return;  // the final swap of sets 0 and 1 is done on the host side
     }
     const bool nhn = variant == kVariantNhn;
@@ -492,11 +631,13 @@ struct Impl final : ImplBase {
     const int sin_slot[3] = {4, 6, 8};
     for (int st = 0; st < 3; ++st) {
       StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing, ctx->prm.forcing_amplitude};
+      // in the compensated state every stage's output set carries the residuals
       mark(MIFGPU_PROF_STAGE, s);
-      launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt);
-      enqueue_bc(ctx, s, out_set[st], 1 + st, cnt);
-      enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt);
-      enqueue_project(s, out_set[st], dts[st], 16u + st, cnt);
+      launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res);
+      enqueue_bc(ctx, s, out_set[st], 1 + st, cnt, res);
+      enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt, res);
+      // the last projection of the step watches phi for NaN / Inf
+      enqueue_project(s, out_set[st], dts[st], 16u + st, cnt, res, st == 2 ? nonfinite : nullptr);
     }
   }
 
@@ -519,6 +660,7 @@ struct Impl final : ImplBase {
 
   int step(mifgpu_ctx *ctx, int variant, const double *host_slots, int nsteps) override {
     if (int rc = ensure_graph(ctx, variant)) return rc;
+    CK(cudaMemsetAsync(nonfinite, 0, sizeof(int), ctx->stream));
     for (int n0 = 0; n0 < nsteps; n0 += slots_cap) {
       const int chunk = std::min(slots_cap, nsteps - n0);
       CK(cudaMemcpyAsync(slots, host_slots + (size_t)kSlotSize * n0, sizeof(double) * kSlotSize * chunk,
@@ -530,7 +672,13 @@ struct Impl final : ImplBase {
       }
     }
     // The host copy of the slots may be a temporary: wait until it was consumed.
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, nonfinite, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (bad)
+      return fail(ctx, MIFGPU_ENONFINITE,
+                  "a projection step produced a NaN or Inf pressure increment (the velocity or pressure is no longer "
+                  "finite)");
     return MIFGPU_OK;
   }
 
@@ -571,13 +719,13 @@ struct Impl final : ImplBase {
 
   int apply_bc(mifgpu_ctx *ctx, int set, double t) override {
     if (int rc = write_single_slot(ctx, t)) return rc;
-    enqueue_bc(ctx, ctx->stream, set, 0, &ctx->launches);
+    enqueue_bc(ctx, ctx->stream, set, 0, &ctx->launches, set_res(set));
     CK(cudaGetLastError());
     return MIFGPU_OK;
   }
 
   int solve_pressure(mifgpu_ctx *ctx, int set, double dt, bool solve) override {
-    enqueue_pressure(ctx, ctx->stream, set, dt, false, 0, 0, solve, &ctx->launches);
+    enqueue_pressure(ctx, ctx->stream, set, dt, false, 0, 0, solve, &ctx->launches, set_res(set));
     CK(cudaGetLastError());
     return MIFGPU_OK;
   }
@@ -586,7 +734,7 @@ struct Impl final : ImplBase {
     // the kernel reads time slot 0 (its rounding draw): point the step
     // counter at a written slot
     if (int rc = write_single_slot(ctx, 0.0)) return rc;
-    enqueue_project(ctx->stream, set, dt, 15u, &ctx->launches);
+    enqueue_project(ctx->stream, set, dt, 15u, &ctx->launches, set_res(set));
     CK(cudaGetLastError());
     return MIFGPU_OK;
   }
@@ -610,7 +758,7 @@ struct Impl final : ImplBase {
     T *gv[3] = {grad_block, grad_block + field_elems, grad_block + 2 * field_elems};
     T *vel[3] = {F.vel(0, 0), F.vel(0, 1), F.vel(0, 2)};
     CK(cudaMemsetAsync(acc, 0, sizeof(double) * 9, ctx->stream));
-    launch_velocity_errors<T>(g, vel, kind, 0, t, acc, ctx->stream, &ctx->launches);
+    launch_velocity_errors<T>(g, vel, kind, 0, t, acc, ctx->stream, &ctx->launches, res);
     launch_pressure_errors<T>(g, F.f[kP], kind, t, acc + 3, ctx->stream, &ctx->launches);
     launch_pressure_gradient<T>(g, gv, F.f[kP], ctx->stream, &ctx->launches);
     if (int rc = write_single_slot(ctx, t)) return rc;
@@ -622,11 +770,7 @@ struct Impl final : ImplBase {
     const double vol = g.h[0] * g.h[1] * g.h[2];
     for (int b = 0; b < 3; ++b) {
       const double *a = h + 3 * b;
-      if (b == 1) {
-        out[3 * b + 0] = a[0] * vol;  // sum |e| (scalar field)
-      } else {
-        out[3 * b + 0] = a[0] * vol;  // sum |e| (vector norm)
-      }
+      out[3 * b + 0] = a[0] * vol;  // sum of |e| (of the error vector for velocity and gradient)
       out[3 * b + 1] = std::sqrt(a[1] * vol);
       out[3 * b + 2] = a[2];
     }
@@ -716,6 +860,8 @@ struct Impl final : ImplBase {
   }
 
   int gradient(mifgpu_ctx *ctx, const GradRequest &req) override {
+    if (res.on())
+      return fail(ctx, MIFGPU_ENOTSUP, "the reverse mode runs in MIFGPU_FP64 or MIFGPU_MIXED, not on a compensated state");
     const int N = req.nsteps;
     const int C = std::max(1, std::min(req.every, N));
     if (C > slots_cap) return fail(ctx, MIFGPU_EINVAL, "checkpoint interval above 1024 steps");
@@ -896,9 +1042,9 @@ int mifgpu_create(const mifgpu_params *p, mifgpu_ctx **out) {
   *out = nullptr;
   auto ctx = std::make_unique<mifgpu_ctx>();
   ctx->prm = *p;
-  if (p->precision != MIFGPU_FP64 && p->precision != MIFGPU_MIXED)
+  if (p->precision != MIFGPU_FP64 && p->precision != MIFGPU_MIXED && p->precision != MIFGPU_MIXED_COMPENSATED)
     return MIFGPU_EINVAL;
-  if (p->boundary_kind < 0 || p->boundary_kind > 2 || p->forcing < 0 || p->forcing > 3) return MIFGPU_EINVAL;
+  if (p->boundary_kind < 0 || p->boundary_kind > 3 || p->forcing < 0 || p->forcing > 3) return MIFGPU_EINVAL;
   if (!(p->Re > 0) || !(p->dt > 0)) return MIFGPU_EINVAL;
   Geometry &g = ctx->g;
   for (int d = 0; d < 3; ++d) {
@@ -995,8 +1141,19 @@ int mifgpu_download(mifgpu_ctx *ctx, int field, double *host) {
   return ctx->impl->download(ctx, field, host);
 }
 
+namespace {
+// Entry points that evaluate the analytic family have nothing to evaluate
+// when the caller supplies the boundary data.
+int needs_family(mifgpu_ctx *ctx, const char *what) {
+  if (ctx->prm.boundary_kind != MIFGPU_FIELD_CALLER) return MIFGPU_OK;
+  return fail(ctx, MIFGPU_ENOTSUP,
+              std::string(what) + " evaluates the analytic family; boundary_kind MIFGPU_FIELD_CALLER has none");
+}
+}  // namespace
+
 int mifgpu_set_exact_velocity(mifgpu_ctx *ctx, int set, double t) {
   if (!ctx || set < 0 || set > 2) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "set_exact_velocity")) return rc;
   for (int c = 0; c < 3; ++c)
     if (int rc = ctx->impl->set_exact(ctx, set * 3 + c, t)) return rc;
   return MIFGPU_OK;
@@ -1004,6 +1161,7 @@ int mifgpu_set_exact_velocity(mifgpu_ctx *ctx, int set, double t) {
 
 int mifgpu_set_exact_pressure(mifgpu_ctx *ctx, double t) {
   if (!ctx) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "set_exact_pressure")) return rc;
   return ctx->impl->set_exact(ctx, kP, t);
 }
 
@@ -1017,6 +1175,9 @@ int mifgpu_timestep(mifgpu_ctx *ctx, double t_n) {
 int mifgpu_run(mifgpu_ctx *ctx, double t0, int nsteps) {
   if (!ctx || nsteps < 0) return MIFGPU_EINVAL;
   if (nsteps == 0) return MIFGPU_OK;
+  if (nsteps > 1 && ctx->prm.boundary_kind == MIFGPU_FIELD_CALLER)
+    return fail(ctx, MIFGPU_ENOTSUP,
+                "with boundary_kind MIFGPU_FIELD_CALLER the boundary data is set per step: run one step at a time");
   std::vector<double> s((size_t)kSlotSize * nsteps);
   for (int n = 0; n < nsteps; ++n)
     projection_slot(t0 + n * ctx->g.dt, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s.data() + (size_t)kSlotSize * n);
@@ -1029,8 +1190,13 @@ int mifgpu_timestep_host(mifgpu_ctx *ctx, double t_n, double *u, double *v, doub
   const double *hc[4] = {u, v, w, p};
   const int ids[4] = {0, 1, 2, kP};
   if (int rc = ctx->impl->upload_fields(ctx, ids, hc, 4)) return rc;
-  if (int rc = mifgpu_timestep(ctx, t_n)) return rc;
-  return ctx->impl->download_fields(ctx, ids, h, 4);
+  const int rc = mifgpu_timestep(ctx, t_n);
+  if (rc != MIFGPU_OK && rc != MIFGPU_ENONFINITE) return rc;
+  // a non-finite step still hands its state back, then reports it
+  const std::string msg = ctx->err;
+  if (int rd = ctx->impl->download_fields(ctx, ids, h, 4)) return rd;
+  if (rc != MIFGPU_OK) ctx->err = msg;
+  return rc;
 }
 
 int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n) {
@@ -1044,11 +1210,38 @@ int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n) {
 
 int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n) {
   if (!ctx) return MIFGPU_EINVAL;
+  if (ctx->prm.precision == MIFGPU_MIXED_COMPENSATED)
+    return fail(ctx, MIFGPU_ENOTSUP, "the velocity-only step runs in MIFGPU_FP64 or MIFGPU_MIXED");
   double s[kSlotSize];
   velocity_slot(t_n, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s);
   if (int rc = ctx->impl->step(ctx, kVariantVelocity, s, 1)) return rc;
   ctx->impl->swap_sets();  // src/TimestepVelocity.cpp:89
   return MIFGPU_OK;
+}
+
+int mifgpu_set_boundary_values(mifgpu_ctx *ctx, int slot, const double *u, const double *v, const double *w) {
+  if (!ctx || !u || !v || !w || slot < 0 || slot > 3) return MIFGPU_EINVAL;
+  const double *vel[3] = {u, v, w};
+  return ctx->impl->set_boundary_values(ctx, slot, vel);
+}
+
+int mifgpu_set_pressure_gradient_faces(mifgpu_ctx *ctx, int slot, const double *const faces[6]) {
+  if (!ctx || !faces || slot < 0 || slot > 3) return MIFGPU_EINVAL;
+  for (int f = 0; f < 6; ++f)
+    if (!faces[f]) return MIFGPU_EINVAL;
+  if (ctx->prm.boundary_kind != MIFGPU_FIELD_CALLER)
+    return fail(ctx, MIFGPU_EINVAL, "set_pressure_gradient_faces needs boundary_kind MIFGPU_FIELD_CALLER");
+  return ctx->impl->set_gradient_faces(ctx, slot, faces);
+}
+
+int mifgpu_solve_pressure_nhn(mifgpu_ctx *ctx, int set, double dt, const double *const faces[6]) {
+  if (!ctx || !faces || set < 0 || set > 2 || !(dt != 0)) return MIFGPU_EINVAL;
+  for (int f = 0; f < 6; ++f)
+    if (!faces[f]) return MIFGPU_EINVAL;
+  if (ctx->g.periodic[0] || ctx->g.periodic[1] || ctx->g.periodic[2])
+    return fail(ctx, MIFGPU_ENOTSUP, "non-homogeneous Neumann data needs every axis non-periodic");
+  if (int rc = ctx->impl->set_gradient_faces(ctx, 0, faces)) return rc;
+  return ctx->impl->solve_pressure_nhn(ctx, set, dt);
 }
 
 int mifgpu_apply_bc(mifgpu_ctx *ctx, int set, double t) {
@@ -1073,11 +1266,13 @@ int mifgpu_project(mifgpu_ctx *ctx, int set, double dt) {
 
 int mifgpu_adjust_pressure(mifgpu_ctx *ctx, double t) {
   if (!ctx) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "adjust_pressure")) return rc;
   return ctx->impl->adjust_pressure(ctx, t);
 }
 
 int mifgpu_error_norms(mifgpu_ctx *ctx, double t, double out[9]) {
   if (!ctx || !out) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "error_norms")) return rc;
   return ctx->impl->error_norms(ctx, t, out);
 }
 
@@ -1089,6 +1284,7 @@ int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIF
 int mifgpu_gradient_ke(mifgpu_ctx *ctx, double t0, int nsteps, int checkpoint_every, const double box[6],
                        double *loss, double *dloss_dalpha, double ms_out[3]) {
   if (!ctx || !box || nsteps < 1 || checkpoint_every < 1) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "the reverse mode")) return rc;
   GradRequest r;
   r.t0 = t0;
   r.nsteps = nsteps;
@@ -1104,6 +1300,7 @@ int mifgpu_backward(mifgpu_ctx *ctx, double t0, int nsteps, int checkpoint_every
                     const double *seed_v, const double *seed_w, const double *seed_p, double *dloss_dalpha,
                     double ms_out[3]) {
   if (!ctx || nsteps < 1 || checkpoint_every < 1) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "the reverse mode")) return rc;
   GradRequest r;
   r.t0 = t0;
   r.nsteps = nsteps;
@@ -1132,13 +1329,15 @@ int mifgpu_set_forcing_amplitude(mifgpu_ctx *ctx, double alpha) {
 
 int mifgpu_velocity_error_norms_noalloc(mifgpu_ctx *ctx, double t, double out[3]) {
   if (!ctx || !out) return MIFGPU_EINVAL;
+  if (int rc = needs_family(ctx, "velocity_error_norms_noalloc")) return rc;
   const Geometry &g = ctx->g;
   const int planes = g.E[2] - 2;
   if (planes > kNoAllocMaxPlanes)
     return fail(ctx, MIFGPU_EINVAL,
                 "velocity_error_norms_noalloc: " + std::to_string(planes) + " interior z planes exceed the " +
-                    std::to_string(kNoAllocMaxPlanes) + " its static scratch holds (z extent at most " +
-                    std::to_string(kNoAllocMaxPlanes + 2) + ")");
+                    std::to_string(kNoAllocMaxPlanes) + " its static scratch holds (n_global[2] at most " +
+                    std::to_string(kNoAllocMaxPlanes + 2) + " on a Dirichlet z axis, " +
+                    std::to_string(kNoAllocMaxPlanes + 1) + " on a periodic one)");
   int cur = -1;
   CK(cudaGetDevice(&cur));
   if (cur != ctx->device) return fail(ctx, MIFGPU_EINVAL, "velocity_error_norms_noalloc: the context's device is not current");
@@ -1150,12 +1349,12 @@ int mifgpu_velocity_error_norms_noalloc(mifgpu_ctx *ctx, double t, double out[3]
     launch_velocity_errors_noalloc<double>(g, (const double *)ctx->impl->field_ptr(0),
                                            (const double *)ctx->impl->field_ptr(1),
                                            (const double *)ctx->impl->field_ptr(2), kind, t, scratch, ctx->stream,
-                                           &ctx->launches);
+                                           &ctx->launches, Residual{});
   else
     launch_velocity_errors_noalloc<float>(g, (const float *)ctx->impl->field_ptr(0),
                                           (const float *)ctx->impl->field_ptr(1),
                                           (const float *)ctx->impl->field_ptr(2), kind, t, scratch, ctx->stream,
-                                          &ctx->launches);
+                                          &ctx->launches, ctx->impl->residual());
   CK(cudaGetLastError());
   double h[3];
   CK(cudaMemcpyAsync(h, scratch + 3 * kNoAllocMaxPlanes, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));

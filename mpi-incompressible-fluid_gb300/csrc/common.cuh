@@ -12,6 +12,7 @@
 // the fused kernels need a single address per point.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -51,6 +52,39 @@ template <typename T>
 struct Coeffs {
   T o2h[3], o8h[3], oh2Re[3], oh[3];
 };
+
+// Compensated float state (MIFGPU_MIXED_COMPENSATED): each velocity
+// component of the state carries a bfloat16 residual, so the value is
+// hi + lo with hi the float field and lo what the float update rounded away
+// (about 32 significant bits in all). One residual triple serves every
+// velocity set: each kernel that writes a state reads the residual of its
+// input state at the same point and overwrites it with the residual of its
+// output state. c[0] == nullptr: no compensation (FP64, MIXED).
+struct Residual {
+  __nv_bfloat16 *c[3] = {nullptr, nullptr, nullptr};
+  __host__ __device__ bool on() const { return c[0] != nullptr; }
+};
+
+// hi + (lo + inc) as an error-free float sum (Knuth's TwoSum on hi and
+// t = lo + inc): returns the new hi and stores the rounding error, rounded to
+// bfloat16, as the new residual. Exact for any magnitudes; the only losses are
+// the float rounding of t (2^-24 |t|, with |t| about ulp(hi) + |inc|) and the
+// bfloat16 rounding of the residual (2^-9 of half an ulp of hi).
+__device__ __forceinline__ float comp_add(float hi, float lo, float inc, __nv_bfloat16 *lo_out) {
+  const float t = __fadd_rn(lo, inc);
+  const float s = __fadd_rn(hi, t);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+  *lo_out = __float2bfloat16_rn(e);
+  return s;
+}
+
+// A double value split into its float part and the bfloat16 residual.
+__device__ __forceinline__ float comp_split(double v, __nv_bfloat16 *lo_out) {
+  const float hi = (float)v;
+  *lo_out = __float2bfloat16_rn((float)(v - (double)hi));
+  return hi;
+}
 
 template <typename T>
 struct Vec2;

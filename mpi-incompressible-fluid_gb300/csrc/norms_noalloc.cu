@@ -46,7 +46,7 @@ __device__ void block_sum2_max(double &a, double &b, double &m) {
 
 template <typename T>
 __global__ void __launch_bounds__(kNT) velocity_error_plane_kernel(Geometry g, const T *u, const T *v, const T *w,
-                                                                   int kind, double t, double *part) {
+                                                                   int kind, double t, double *part, Residual res) {
   const long ni = g.E[0] - 2, nj = g.E[1] - 2;
   const long k = 1 + blockIdx.x;
   double a = 0, b = 0, m = 0;
@@ -56,9 +56,13 @@ __global__ void __launch_bounds__(kNT) velocity_error_plane_kernel(Geometry g, c
     const double x = g.origin[0] + (double)(g.base[0] + i) * g.h[0];
     const double y = g.origin[1] + (double)(g.base[1] + j) * g.h[1];
     const double z = g.origin[2] + (double)(g.base[2] + k) * g.h[2];
-    const double iu = ((double)u[q] + (double)u[q + 1]) / 2.0;
-    const double iv = ((double)v[q] + (double)v[q + g.sy()]) / 2.0;
-    const double iw = ((double)w[q] + (double)w[q + g.sz()]) / 2.0;
+    // the compensated state's value is hi + residual
+    auto val = [&](const T *f, int c, long qq) {
+      return res.on() ? (double)f[qq] + (double)__bfloat162float(res.c[c][qq]) : (double)f[qq];
+    };
+    const double iu = (val(u, 0, q) + val(u, 0, q + 1)) / 2.0;
+    const double iv = (val(v, 1, q) + val(v, 1, q + g.sy())) / 2.0;
+    const double iw = (val(w, 2, q) + val(w, 2, q + g.sz())) / 2.0;
     const double eu = analytic_value<double>(kind, 0, t, x, y, z, g.Re) - iu;
     const double ev = analytic_value<double>(kind, 1, t, x, y, z, g.Re) - iv;
     const double ew = analytic_value<double>(kind, 2, t, x, y, z, g.Re) - iw;
@@ -91,9 +95,34 @@ __global__ void __launch_bounds__(kNT) plane_totals_kernel(const double *part, i
 
 }  // namespace
 
+// The unique id of the current context (cuCtxGetId, reached through the
+// runtime's driver entry point so the library needs no libcuda link), or 0
+// if the driver cannot tell.
+unsigned long long current_context_id() {
+  using GetId = int (*)(void *, unsigned long long *);  // CUresult cuCtxGetId(CUcontext, unsigned long long *)
+  static GetId fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (GetId) nullptr;
+    return reinterpret_cast<GetId>(p);
+  }();
+  unsigned long long id = 0;
+  if (!fn || fn(nullptr, &id) != 0) return 0;
+  return id;
+}
+
 int noalloc_scratch(double **out, std::string &err) {
+  // Per device: the context the address was looked up in and the address. A
+  // new context on the device (after cudaDeviceReset, say) reloads the
+  // module and may move the array, so the lookup is repeated for it.
+  struct Entry {
+    unsigned long long ctx;
+    void *addr;
+  };
   static std::mutex mu;
-  static void *addr[kMaxDevices] = {};
+  static Entry cache[kMaxDevices] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
@@ -104,33 +133,35 @@ int noalloc_scratch(double **out, std::string &err) {
     err = "device index beyond the scratch address cache";
     return -2;
   }
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
+  if (!cache[dev].addr || cache[dev].ctx != ctx) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_norm_scratch);
     if (e != cudaSuccess) {
       err = std::string("cudaGetSymbolAddress of the norm scratch: ") + cudaGetErrorString(e);
       return -2;
     }
-    addr[dev] = p;
+    cache[dev] = Entry{ctx, p};
   }
-  *out = static_cast<double *>(addr[dev]);
+  *out = static_cast<double *>(cache[dev].addr);
   return 0;
 }
 
 template <typename T>
 void launch_velocity_errors_noalloc(const Geometry &g, const T *u, const T *v, const T *w, int field_kind, double t,
-                                    double *scratch, cudaStream_t s, long long *launches) {
+                                    double *scratch, cudaStream_t s, long long *launches, const Residual &res) {
   const int planes = g.E[2] - 2;
-  velocity_error_plane_kernel<T><<<planes, kNT, 0, s>>>(g, u, v, w, field_kind, t, scratch);
+  velocity_error_plane_kernel<T><<<planes, kNT, 0, s>>>(g, u, v, w, field_kind, t, scratch, res);
   plane_totals_kernel<<<1, kNT, 0, s>>>(scratch, planes, scratch + 3 * kNoAllocMaxPlanes);
   if (launches) *launches += 2;
 }
 
 template void launch_velocity_errors_noalloc<float>(const Geometry &, const float *, const float *, const float *,
-                                                    int, double, double *, cudaStream_t, long long *);
+                                                    int, double, double *, cudaStream_t, long long *,
+                                                    const Residual &);
 template void launch_velocity_errors_noalloc<double>(const Geometry &, const double *, const double *,
                                                      const double *, int, double, double *, cudaStream_t,
-                                                     long long *);
+                                                     long long *, const Residual &);
 
 }  // namespace mifgpu

@@ -278,10 +278,13 @@ __device__ __forceinline__ T rhs_taps(int c, const Taps<T> &a, const Coeffs<T> &
 // 2 / 3 / 4 / 5 / 6 / 8 CTAs of 32 x 8 threads per SM, and 4.44 ms for twelve
 // CTAs of 32 x 4 (half the threads per barrier, 20 % more halo rows). FP64:
 // 8 warps per SM.
-template <typename T, int ST>
-__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4) stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K,
-                                                              int forcing, ForcingEval<T> fe, TimeRef tr, int sin_slot,
-                                                              int kc) {
+// kComp (float only, projection stages): the input state is hi + residual
+// and the output state is written as an error-free sum (comp_add) into its
+// float field and the residual, in place (Residual).
+template <typename T, int ST, bool kComp>
+__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4)
+    stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K, int forcing, ForcingEval<T> fe,
+                       TimeRef tr, int sin_slot, int kc, Residual res) {
   constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
   constexpr int in_set = (ST == kStageY2 || ST == kVelY2 || ST == kVelUStar) ? 0
                          : (ST == kStageY3 || ST == kVelY3)                  ? 1
@@ -354,6 +357,8 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4) stage_kerne
   constexpr bool kPre0 = ST == kStageUStar || ST == kVelY3;
   const bool in_box = i < g.PX && j < g.PY;
   T n2[3] = {T(0), T(0), T(0)}, n0[3] = {T(0), T(0), T(0)};
+  // the input state's residual at the point, prefetched the same way
+  __nv_bfloat16 nl[3] = {__float2bfloat16_rn(0.f), __float2bfloat16_rn(0.f), __float2bfloat16_rn(0.f)};
   auto prefetch = [&](int kk) {
     if (!in_box || kk >= kend) return;
     const long qq = g.idx(i, j, kk);
@@ -361,6 +366,7 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4) stage_kerne
     for (int c = 0; c < 3; ++c) {
       if (kPre2) n2[c] = F.vel(2, c)[qq];
       if (kPre0) n0[c] = F.vel(0, c)[qq];
+      if constexpr (kComp) nl[c] = res.c[c][qq];
     }
   };
   prefetch(kbeg);
@@ -378,10 +384,12 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4) stage_kerne
     load_plane(k + 2);
     if (forcing) fz = fe.axis(2, k);
     T c2[3], c0[3];
+    __nv_bfloat16 cl[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       c2[c] = n2[c];
       c0[c] = n0[c];
+      cl[c] = nl[c];
     }
     prefetch(k + 1);
     cp_wait1();
@@ -401,6 +409,22 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4) stage_kerne
       T gp = T(0);
       if (kUseP) gp = tp.dp(c) * co.oh[c];
       const T self = tp.self(c);  // the input set's own value at the point
+      if constexpr (kComp) {
+        // the same increments as below, added to hi + residual without loss
+        const float lo = __bfloat162float(cl[c]);
+        __nv_bfloat16 *lo_out = res.c[c] + q;
+        if constexpr (ST == kStageY2) {
+          F.vel(1, c)[q] = comp_add(self, lo, K.k1 * r - K.k3 * gp, lo_out);
+          F.vel(2, c)[q] = r;
+        } else if constexpr (ST == kStageY3) {
+          const T r2s = K.k2 * r;
+          F.vel(2, c)[q] = comp_add(self, lo, K.k1 * c2[c] + r2s - K.k3 * gp, lo_out);
+          F.vel(0, c)[q] = r2s;
+        } else {
+          F.vel(0, c)[q] = comp_add(self, lo, -c0[c] + K.k2 * r - K.k3 * gp, lo_out);
+        }
+        continue;
+      }
       // FP64 keeps the reference's expression order; the float path adds the
       // increment to the state with stochastic rounding
       constexpr bool kSR = std::is_same<T, float>::value;
@@ -483,10 +507,12 @@ __device__ TE face_value(const Geometry &g, int c, int d, int s, const long *pt,
 // z_min, z_max, y_min, y_max, x_min, x_max).
 template <typename T>
 __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int fn, TimeRef tr, int t_slot,
-                                FaceTables ft) {
+                                FaceTables ft, Residual res) {
   const int c = blockIdx.z / 3, d = blockIdx.z % 3;
   const double t = tr.get(t_slot);
-  const double factor = ft.tab ? tr.get(kSlotFactor + 4 * fn + t_slot) : 0.0;
+  // caller data (slot_stride > 0): the slot's own table, no time factor
+  const double factor = ft.tab ? (ft.slot_stride ? 1.0 : tr.get(kSlotFactor + 4 * fn + t_slot)) : 0.0;
+  const double *tab = ft.tab ? ft.tab + (long)t_slot * ft.slot_stride : nullptr;
   if (g.periodic[d]) return;
   const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
   const long pa = blockIdx.x * blockDim.x + threadIdx.x;
@@ -502,9 +528,18 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
     for (int d2 = 0; d2 < d; ++d2)
       if (!g.periodic[d2] && (pt[d2] == 0 || pt[d2] == g.ext(c, d2) - 1)) later = true;
     if (later) continue;
-    const T val = ft.tab ? T(ft.tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor)
-                         : T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
-    f[g.idx(pt[0], pt[1], pt[2])] = val;
+    const long q = g.idx(pt[0], pt[1], pt[2]);
+    if constexpr (std::is_same<T, float>::value) {
+      if (res.on()) {  // compensated state: the double face value as hi + residual
+        const double v = tab ? tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor
+                             : (double)face_value<T>(g, c, d, s, pt, kind, fn, T(t));
+        f[q] = comp_split(v, res.c[c] + q);
+        continue;
+      }
+    }
+    const T val = tab ? T(tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor)
+                      : T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
+    f[q] = val;
   }
 }
 
@@ -518,7 +553,7 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
 // ghost plane 0 / E-1 of periodic axis d, a point counted only on its first
 // ghost axis.
 template <typename T>
-__global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int scalar) {
+__global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int scalar, Residual res) {
   const int c = blockIdx.z / 6, face = blockIdx.z % 6, d = face / 2, side = face % 2;
   T *f = c == 0 ? f0 : (c == 1 ? f1 : f2);
   if (!f || !g.periodic[d]) return;
@@ -539,28 +574,39 @@ __global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int scalar) {
     if (ghost && ax < d) return;  // counted on an earlier axis's ghost plane
     q[ax] = !ghost ? p[ax] : (p[ax] == 0 ? ex[ax] - 2 : 1);
   }
-  f[g.idx(p[0], p[1], p[2])] = f[g.idx(q[0], q[1], q[2])];
+  const long dst = g.idx(p[0], p[1], p[2]), src = g.idx(q[0], q[1], q[2]);
+  f[dst] = f[src];
+  if (res.on() && !scalar) res.c[c][dst] = res.c[c][src];
 }
 
 // ---- Poisson right-hand side and projection ----
 
-// Each thread owns kDivKZ consecutive owner planes of one (i, j) column; the
+// Each thread owns KZ consecutive owner planes of one (i, j) column; the
 // loads of all its points are issued before any result is stored.
 constexpr int kDivKZ = 4;
+// The compensated variant reads five more values per point (the residuals):
+// two planes per thread keep it near the plain kernel's register count.
+constexpr int kDivKZComp = 2;
 
-template <typename T>
+// kComp: the velocity is hi + residual; each difference adds the residuals'
+// difference, so the float divergence sees the compensated state.
+template <typename T, bool kComp, int KZ = kComp ? kDivKZComp : kDivKZ>
 __global__ void __launch_bounds__(128) divergence_kernel(Geometry g, T *__restrict__ phi, const T *__restrict__ u,
-                                                         const T *__restrict__ v, const T *__restrict__ w, T inv_dt) {
+                                                         const T *__restrict__ v, const T *__restrict__ w, T inv_dt,
+                                                         Residual res) {
   const int i = g.own_lo[0] + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = g.own_lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
-  const int kb = g.own_lo[2] + blockIdx.z * kDivKZ;
-  const int ke = min(kb + kDivKZ, g.own_lo[2] + g.np[2]);
+  const int kb = g.own_lo[2] + blockIdx.z * KZ;
+  const int ke = min(kb + KZ, g.own_lo[2] + g.np[2]);
   if (i >= g.own_lo[0] + g.np[0] || j >= g.own_lo[1] + g.np[1]) return;
   const long q0 = g.idx(i, j, kb), sy = g.sy(), sz = g.sz();
-  T a[kDivKZ], b[kDivKZ], c[kDivKZ], d[kDivKZ], e[kDivKZ + 1];
+  T a[KZ], b[KZ], c[KZ], d[KZ], e[KZ + 1];
+  float la[KZ], lb[KZ], lc[KZ], ldd[KZ], le[KZ + 1];
+  auto rl = [&](int comp, long q) { return __bfloat162float(__ldg(res.c[comp] + q)); };
   e[0] = ld(w, q0);
+  if constexpr (kComp) le[0] = rl(2, q0);
 #pragma unroll
-  for (int r = 0; r < kDivKZ; ++r) {
+  for (int r = 0; r < KZ; ++r) {
     if (kb + r >= ke) break;
     const long q = q0 + r * sz;
     a[r] = ld(u, q + 1);
@@ -568,13 +614,26 @@ __global__ void __launch_bounds__(128) divergence_kernel(Geometry g, T *__restri
     c[r] = ld(v, q + sy);
     d[r] = ld(v, q);
     e[r + 1] = ld(w, q + sz);
+    if constexpr (kComp) {
+      la[r] = rl(0, q + 1);
+      lb[r] = rl(0, q);
+      lc[r] = rl(1, q + sy);
+      ldd[r] = rl(1, q);
+      le[r + 1] = rl(2, q + sz);
+    }
   }
 #pragma unroll
-  for (int r = 0; r < kDivKZ; ++r) {
+  for (int r = 0; r < KZ; ++r) {
     if (kb + r >= ke) break;
-    const T du = (a[r] - b[r]) * T(g.oh[0]);
-    const T dv = (c[r] - d[r]) * T(g.oh[1]);
-    const T dw = (e[r + 1] - e[r]) * T(g.oh[2]);
+    T du = a[r] - b[r], dv = c[r] - d[r], dw = e[r + 1] - e[r];
+    if constexpr (kComp) {
+      du += la[r] - lb[r];
+      dv += lc[r] - ldd[r];
+      dw += le[r + 1] - le[r];
+    }
+    du = du * T(g.oh[0]);
+    dv = dv * T(g.oh[1]);
+    dw = dw * T(g.oh[2]);
     phi[q0 + r * sz] = (du + dv + dw) * inv_dt;
   }
 }
@@ -606,15 +665,51 @@ __global__ void neumann_flux_serial_kernel(Geometry g, T *phi, int kind, TimeRef
   phi[q] = r;
 }
 
+// Boundary nodes from caller data. blockIdx.z = f, the face (x_min, x_max,
+// y_min, y_max, z_min, z_max) whose threads own its nodes; a node on several
+// faces belongs to the first of them in that order, and its one thread adds
+// the terms of all its faces in the reference's order (z, then y, then x
+// faces, each min before max), so every node is written once.
+template <typename T>
+__global__ void neumann_flux_data_kernel(Geometry g, T *phi, const double *G, GradFaces gf) {
+  const int f = blockIdx.z, d = f / 2, side = f % 2;
+  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+  const long pa = blockIdx.x * blockDim.x + threadIdx.x, pb = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pa >= g.E[a] || pb >= g.E[b]) return;
+  long p[3];
+  p[d] = side ? g.E[d] - 1 : 0;
+  p[a] = pa;
+  p[b] = pb;
+  for (int d2 = 0; d2 < d; ++d2)
+    if (p[d2] == 0 || p[d2] == g.E[d2] - 1) return;  // owned by an x (or y) face
+  if (side == 1 && p[d] == 0) return;
+  const long i = p[0], j = p[1], k = p[2];
+  const long E0 = g.E[0], E1 = g.E[1];
+  const long q = g.idx(i, j, k);
+  T r = phi[q];
+  if (k == 0) r += T(G[gf.off[4] + i + E0 * j]) * T(2.0) * T(g.oh[2]);
+  if (k == g.E[2] - 1) r -= T(G[gf.off[5] + i + E0 * j]) * T(2.0) * T(g.oh[2]);
+  if (j == 0) r += T(G[gf.off[2] + i + E0 * k]) * T(2.0) * T(g.oh[1]);
+  if (j == g.E[1] - 1) r -= T(G[gf.off[3] + i + E0 * k]) * T(2.0) * T(g.oh[1]);
+  if (i == 0) r += T(G[gf.off[0] + j + E1 * k]) * T(2.0) * T(g.oh[0]);
+  if (i == g.E[0] - 1) r -= T(G[gf.off[1] + j + E1 * k]) * T(2.0) * T(g.oh[0]);
+  phi[q] = r;
+}
+
 // Each thread owns kProjKZ consecutive planes of one (i, j) column. Two
 // planes keep it at 32 registers (full occupancy); on GB300 at 512^3 the
 // projection measured 2.76 / 2.44 / 2.77 / 3.13 ms per step for 1 / 2 / 4 / 8.
 constexpr int kProjKZ = 2;
 
-template <typename T>
+// kComp: the velocity update is an error-free sum into hi + residual.
+// nonfinite (may be null): set to 1 when a phi value read is NaN or Inf. A
+// NaN or Inf anywhere in the velocity reaches every phi value through the
+// divergence and the spectral solve, so this one check per point watches
+// the whole step.
+template <typename T, bool kComp>
 __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict__ p, const T *__restrict__ phi,
                                                       T *__restrict__ u, T *__restrict__ v, T *__restrict__ w, T dt,
-                                                      TimeRef tr, unsigned tag) {
+                                                      TimeRef tr, unsigned tag, Residual res, int *nonfinite) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int kb = blockIdx.z * kProjKZ;
@@ -622,6 +717,7 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
   T *vel[3] = {u, v, w};
   const long sc[3] = {1, sy, sz};
   T ph[kProjKZ + 1], nb[2][kProjKZ], pv[kProjKZ], vv[3][kProjKZ];
+  float lv[3][kProjKZ];
   // loads: phi at the points, their -x and -y neighbours, the plane below, p and the velocity
   ph[0] = (kb >= 1 && i < g.E[0] && j < g.E[1] && kb - 1 < g.E[2]) ? ld(phi, g.idx(i, j, kb - 1)) : T(0);
 #pragma unroll
@@ -637,10 +733,17 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
     for (int c = 0; c < 3; ++c) {
       const bool in = i >= 1 && j >= 1 && k >= 1 && i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
       vv[c][r] = in ? vel[c][q] : T(0);
+      if constexpr (kComp) lv[c][r] = in ? __bfloat162float(res.c[c][q]) : 0.f;
     }
   }
   constexpr bool kSR = std::is_same<T, float>::value;
   const unsigned salt = kSR ? sr_salt(tr, tag) : 0u;
+  if (nonfinite) {
+    bool bad = false;
+#pragma unroll
+    for (int r = 0; r <= kProjKZ; ++r) bad |= !isfinite(ph[r]);
+    if (bad) *nonfinite = 1;
+  }
 #pragma unroll
   for (int r = 0; r < kProjKZ; ++r) {
     const int k = kb + r;
@@ -654,7 +757,10 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
       if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
       const T below = c == 0 ? nb[0][r] : (c == 1 ? nb[1][r] : ph[r]);
       const T gp = (ph[r + 1] - below) * T(g.oh[c]);
-      vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_draw(h, c)) : vv[c][r] - gp * dt;
+      if constexpr (kComp)
+        vel[c][q] = comp_add(vv[c][r], lv[c][r], -(gp * dt), res.c[c] + q);
+      else
+        vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_draw(h, c)) : vv[c][r] - gp * dt;
     }
   }
   (void)sc;
@@ -662,26 +768,39 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
 
 // ---- layout conversion and initial fields ----
 
+// lo (float path, compensated state): the residual array of the field, or null.
 template <typename T>
-__global__ void scatter_kernel(Geometry g, T *dst, const double *src, int ex, int ey, int ez) {
+__global__ void scatter_kernel(Geometry g, T *dst, const double *src, int ex, int ey, int ez, __nv_bfloat16 *lo) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= ex || j >= ey) return;
-  dst[g.idx(i, j, k)] = T(src[i + (long)ex * (j + (long)ey * k)]);
+  const long q = g.idx(i, j, k);
+  const double v = src[i + (long)ex * (j + (long)ey * k)];
+  if constexpr (std::is_same<T, float>::value) {
+    if (lo) {
+      dst[q] = comp_split(v, lo + q);
+      return;
+    }
+  }
+  dst[q] = T(v);
 }
 
 template <typename T>
-__global__ void gather_kernel(Geometry g, double *dst, const T *src, int ex, int ey, int ez) {
+__global__ void gather_kernel(Geometry g, double *dst, const T *src, int ex, int ey, int ez,
+                              const __nv_bfloat16 *lo) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= ex || j >= ey) return;
-  dst[i + (long)ex * (j + (long)ey * k)] = double(src[g.idx(i, j, k)]);
+  const long q = g.idx(i, j, k);
+  double v = double(src[q]);
+  if (lo) v += (double)__bfloat162float(lo[q]);
+  dst[i + (long)ex * (j + (long)ey * k)] = v;
 }
 
 template <typename T>
-__global__ void set_exact_kernel(Geometry g, T *f, int comp, int kind, double t, int ex, int ey) {
+__global__ void set_exact_kernel(Geometry g, T *f, int comp, int kind, double t, int ex, int ey, __nv_bfloat16 *lo) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -689,7 +808,15 @@ __global__ void set_exact_kernel(Geometry g, T *f, int comp, int kind, double t,
   const long pt[3] = {i, j, k};
   double x[3];
   stag_point(g, comp, pt, x);  // comp 3 (pressure): every axis at nodes
-  f[g.idx(i, j, k)] = T(analytic_value<double>(kind, comp, t, x[0], x[1], x[2], g.Re));
+  const long q = g.idx(i, j, k);
+  const double v = analytic_value<double>(kind, comp, t, x[0], x[1], x[2], g.Re);
+  if constexpr (std::is_same<T, float>::value) {
+    if (lo) {
+      f[q] = comp_split(v, lo + q);
+      return;
+    }
+  }
+  f[q] = T(v);
 }
 
 // ---- double-precision reductions ----
@@ -732,7 +859,7 @@ __device__ void block_reduce3(double a, double b, double m, double *acc) {
 // src/Norms.cpp:11-47: velocity interpolated to interior nodes vs the family.
 template <typename T>
 __global__ void __launch_bounds__(256) velocity_error_kernel(Geometry g, const T *u, const T *v, const T *w, int kind,
-                                                             int fn, double t, double *acc) {
+                                                             int fn, double t, double *acc, Residual res) {
   const long ni = g.E[0] - 2, nj = g.E[1] - 2, nk = g.E[2] - 2;
   const long n = ni * nj * nk;
   double a = 0, b = 0, m = 0;
@@ -742,9 +869,13 @@ __global__ void __launch_bounds__(256) velocity_error_kernel(Geometry g, const T
     const double x = g.origin[0] + (double)(g.base[0] + i) * g.h[0];
     const double y = g.origin[1] + (double)(g.base[1] + j) * g.h[1];
     const double z = g.origin[2] + (double)(g.base[2] + k) * g.h[2];
-    const double iu = ((double)u[q] + (double)u[q + 1]) / 2.0;
-    const double iv = ((double)v[q] + (double)v[q + g.sy()]) / 2.0;
-    const double iw = ((double)w[q] + (double)w[q + g.sz()]) / 2.0;
+    // the compensated state's value is hi + residual
+    auto val = [&](const T *f, int c, long qq) {
+      return res.on() ? (double)f[qq] + (double)__bfloat162float(res.c[c][qq]) : (double)f[qq];
+    };
+    const double iu = (val(u, 0, q) + val(u, 0, q + 1)) / 2.0;
+    const double iv = (val(v, 1, q) + val(v, 1, q + g.sy())) / 2.0;
+    const double iw = (val(w, 2, q) + val(w, 2, q + g.sz())) / 2.0;
     const double eu = analytic_vector<double>(fn, kind, 0, t, x, y, z, g.Re) - iu;
     const double ev = analytic_vector<double>(fn, kind, 1, t, x, y, z, g.Re) - iv;
     const double ew = analytic_vector<double>(fn, kind, 2, t, x, y, z, g.Re) - iw;
@@ -814,15 +945,6 @@ __global__ void pressure_gradient_kernel(Geometry g, T *u, T *v, T *w, const T *
   }
 }
 
-template <typename T>
-__global__ void nonfinite_kernel(const T *f, long n, int *flag) {
-  for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (long)gridDim.x * blockDim.x)
-    if (!isfinite(f[id])) {
-      *flag = 1;
-      return;
-    }
-}
-
 inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
 
 template <typename T>
@@ -837,13 +959,40 @@ Coeffs<T> make_coeffs(const Geometry &g) {
   return c;
 }
 
+// One stage launch; the compensated variant exists for the float projection stages only.
+template <typename T>
+struct StageLaunch {
+  dim3 grid, blk;
+  cudaStream_t s;
+  Geometry g;
+  Coeffs<T> co;
+  Fields<T> F;
+  StageCoef<T> K;
+  int forcing;
+  ForcingEval<T> fe;
+  TimeRef tr;
+  int sin_slot, kc;
+  Residual res;
+  template <int ST>
+  void go(bool comp) const {
+    if constexpr (std::is_same<T, float>::value && ST <= kStageUStar) {
+      if (comp) {
+        stage_kernel_tiled<T, ST, true><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res);
+        return;
+      }
+    }
+    stage_kernel_tiled<T, ST, false><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res);
+  }
+};
+
 }  // namespace
 
 // ---- launchers ----
 
 template <typename T>
 void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
-                  const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches) {
+                  const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches,
+                  const Residual &res) {
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
   const int nk = g.Es[2] - 2;
   // Planes per CTA: 32, halved (down to 4) while the grid would not fill the
@@ -903,31 +1052,34 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   const int forcing = ft.tab != nullptr && ((sc.forcing == 1 || sc.forcing == 2) ? field_kind == kFieldSincos
                                                                                   : sc.forcing == 3);
   const Coeffs<T> co = make_coeffs<T>(g);
+  const dim3 blk(kTX * kTY);
+  const bool comp = res.on() && st <= kStageUStar;
+  const StageLaunch<T> L{tgrid, blk, s, g, co, F, K, forcing, fe, tr, sc.sin_slot, kc, res};
   switch (st) {
-    case kStageY2: stage_kernel_tiled<T, kStageY2><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
-    case kStageY3: stage_kernel_tiled<T, kStageY3><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
-    case kStageUStar: stage_kernel_tiled<T, kStageUStar><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
-    case kVelY2: stage_kernel_tiled<T, kVelY2><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
-    case kVelY3: stage_kernel_tiled<T, kVelY3><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
-    default: stage_kernel_tiled<T, kVelUStar><<<tgrid, kTX * kTY, 0, s>>>(g, co, F, K, forcing, fe, tr, sc.sin_slot, kc); break;
+    case kStageY2: L.template go<kStageY2>(comp); break;
+    case kStageY3: L.template go<kStageY3>(comp); break;
+    case kStageUStar: L.template go<kStageUStar>(comp); break;
+    case kVelY2: L.template go<kVelY2>(false); break;
+    case kVelY3: L.template go<kVelY3>(false); break;
+    default: L.template go<kVelUStar>(false); break;
   }
   if (launches) ++*launches;
 }
 
 template <typename T>
 void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn, TimeRef tr, int t_slot,
-                     const FaceTables &ft, cudaStream_t s, long long *launches) {
+                     const FaceTables &ft, cudaStream_t s, long long *launches, const Residual &res) {
   const dim3 blk(32, 8, 1);
   int mx = 0;
   for (int d = 0; d < 3; ++d) mx = mx > g.Es[d] ? mx : g.Es[d];
   if (!(g.periodic[0] && g.periodic[1] && g.periodic[2])) {
     const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 9);
-    bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft);
+    bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft, res);
     if (launches) ++*launches;
   }
   if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {
     const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 18);
-    periodic_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], 0);
+    periodic_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], 0, res);
     if (launches) ++*launches;
   }
 }
@@ -979,16 +1131,23 @@ void launch_periodic_scalar(const Geometry &g, T *f, cudaStream_t s, long long *
   for (int d = 0; d < 3; ++d) mx = mx > g.E[d] ? mx : g.E[d];
   if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {
     const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 6);
-    periodic_kernel<T><<<grid, blk, 0, s>>>(g, f, nullptr, nullptr, 1);
+    periodic_kernel<T><<<grid, blk, 0, s>>>(g, f, nullptr, nullptr, 1, Residual{});
     if (launches) ++*launches;
   }
 }
 
 template <typename T>
-void launch_divergence(const Geometry &g, T *phi, T *const vel[3], double dt, cudaStream_t s, long long *launches) {
+void launch_divergence(const Geometry &g, T *phi, T *const vel[3], double dt, cudaStream_t s, long long *launches,
+                       const Residual &res) {
   const dim3 blk(32, 4, 1);
-  const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZ));
-  divergence_kernel<T><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt));
+  if (std::is_same<T, float>::value && res.on()) {
+    const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZComp));
+    divergence_kernel<T, std::is_same<T, float>::value><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2],
+                                                                             T(1.0 / dt), res);
+  } else {
+    const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZ));
+    divergence_kernel<T, false><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt), res);
+  }
   if (launches) ++*launches;
 }
 
@@ -1001,39 +1160,54 @@ void launch_neumann_flux(const Geometry &g, T *phi, int field_kind, TimeRef tr, 
 }
 
 template <typename T>
+void launch_neumann_flux_data(const Geometry &g, T *phi, const GradFaces &gf, int slot, cudaStream_t s,
+                              long long *launches) {
+  int mx = 0;
+  for (int d = 0; d < 3; ++d) mx = mx > g.E[d] ? mx : g.E[d];
+  const dim3 blk(32, 8, 1), grid(cdiv(mx, 32), cdiv(mx, 8), 6);
+  neumann_flux_data_kernel<T><<<grid, blk, 0, s>>>(g, phi, gf.tab + (long)slot * gf.slot_stride, gf);
+  if (launches) ++*launches;
+}
+
+template <typename T>
 void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], double dt, TimeRef tr, unsigned tag,
-                    cudaStream_t s, long long *launches) {
+                    cudaStream_t s, long long *launches, const Residual &res, int *nonfinite) {
   const dim3 blk(32, 4, 1);
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
   const dim3 grid(cdiv(ni, 32), cdiv(g.Es[1], 4), cdiv(g.Es[2], kProjKZ));
-  project_kernel<T><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt), tr, tag);
+  if (std::is_same<T, float>::value && res.on())
+    project_kernel<T, std::is_same<T, float>::value><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt),
+                                                                          tr, tag, res, nonfinite);
+  else
+    project_kernel<T, false><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt), tr, tag, res,
+                                                  nonfinite);
   if (launches) ++*launches;
 }
 
 template <typename T>
 void launch_scatter(const Geometry &g, T *dst, const double *src, int ex, int ey, int ez, cudaStream_t s,
-                    long long *launches) {
+                    long long *launches, __nv_bfloat16 *lo) {
   const dim3 blk(32, 8, 1), grid(cdiv(ex, 32), cdiv(ey, 8), (unsigned)ez);
-  scatter_kernel<T><<<grid, blk, 0, s>>>(g, dst, src, ex, ey, ez);
+  scatter_kernel<T><<<grid, blk, 0, s>>>(g, dst, src, ex, ey, ez, lo);
   if (launches) ++*launches;
 }
 
 template <typename T>
 void launch_gather(const Geometry &g, double *dst, const T *src, int ex, int ey, int ez, cudaStream_t s,
-                   long long *launches) {
+                   long long *launches, const __nv_bfloat16 *lo) {
   const dim3 blk(32, 8, 1), grid(cdiv(ex, 32), cdiv(ey, 8), (unsigned)ez);
-  gather_kernel<T><<<grid, blk, 0, s>>>(g, dst, src, ex, ey, ez);
+  gather_kernel<T><<<grid, blk, 0, s>>>(g, dst, src, ex, ey, ez, lo);
   if (launches) ++*launches;
 }
 
 template <typename T>
 void launch_set_exact(const Geometry &g, T *f, int comp, int field_kind, double t, cudaStream_t s,
-                      long long *launches) {
+                      long long *launches, __nv_bfloat16 *lo) {
   const int ex = comp < 3 ? g.ext(comp, 0) : g.E[0];
   const int ey = comp < 3 ? g.ext(comp, 1) : g.E[1];
   const int ez = comp < 3 ? g.ext(comp, 2) : g.E[2];
   const dim3 blk(32, 8, 1), grid(cdiv(ex, 32), cdiv(ey, 8), (unsigned)ez);
-  set_exact_kernel<T><<<grid, blk, 0, s>>>(g, f, comp, field_kind, t, ex, ey);
+  set_exact_kernel<T><<<grid, blk, 0, s>>>(g, f, comp, field_kind, t, ex, ey, lo);
   if (launches) ++*launches;
 }
 
@@ -1054,8 +1228,8 @@ void launch_add_scalar(const Geometry &g, T *p, const double *shift, cudaStream_
 
 template <typename T>
 void launch_velocity_errors(const Geometry &g, T *const vel[3], int field_kind, int fn, double t, double *acc,
-                            cudaStream_t s, long long *launches) {
-  velocity_error_kernel<T><<<1024, 256, 0, s>>>(g, vel[0], vel[1], vel[2], field_kind, fn, t, acc);
+                            cudaStream_t s, long long *launches, const Residual &res) {
+  velocity_error_kernel<T><<<1024, 256, 0, s>>>(g, vel[0], vel[1], vel[2], field_kind, fn, t, acc, res);
   if (launches) ++*launches;
 }
 
@@ -1075,33 +1249,33 @@ void launch_pressure_gradient(const Geometry &g, T *const vel[3], const T *p, cu
   if (launches) ++*launches;
 }
 
-template <typename T>
-void launch_nonfinite_check(const T *f, long n, int *flag, cudaStream_t s, long long *launches) {
-  nonfinite_kernel<T><<<1024, 256, 0, s>>>(f, n, flag);
-  if (launches) ++*launches;
-}
-
 #define MIFGPU_INSTANTIATE(T)                                                                                        \
   template void launch_stage<T>(const Geometry &, const Fields<T> &, StageKind, const StageScalars<T> &,             \
-                                const ForcingTables<T> &, int, TimeRef, cudaStream_t, long long *);                  \
+                                const ForcingTables<T> &, int, TimeRef, cudaStream_t, long long *,                   \
+                                const Residual &);                                                                   \
   template void launch_apply_bc<T>(const Geometry &, T *const[3], int, int, TimeRef, int, const FaceTables &,     \
-                                   cudaStream_t, long long *);                                                    \
+                                   cudaStream_t, long long *, const Residual &);                                  \
   template void launch_periodic_scalar<T>(const Geometry &, T *, cudaStream_t, long long *);                       \
-  template void launch_divergence<T>(const Geometry &, T *, T *const[3], double, cudaStream_t, long long *);       \
+  template void launch_divergence<T>(const Geometry &, T *, T *const[3], double, cudaStream_t, long long *,       \
+                                     const Residual &);                                                            \
   template void launch_neumann_flux<T>(const Geometry &, T *, int, TimeRef, int, int, cudaStream_t, long long *);  \
+  template void launch_neumann_flux_data<T>(const Geometry &, T *, const GradFaces &, int, cudaStream_t,            \
+                                            long long *);                                                         \
   template void launch_project<T>(const Geometry &, T *, const T *, T *const[3], double, TimeRef, unsigned,      \
-                                  cudaStream_t, long long *);                                                     \
-  template void launch_scatter<T>(const Geometry &, T *, const double *, int, int, int, cudaStream_t, long long *); \
-  template void launch_gather<T>(const Geometry &, double *, const T *, int, int, int, cudaStream_t, long long *);  \
-  template void launch_set_exact<T>(const Geometry &, T *, int, int, double, cudaStream_t, long long *);           \
+                                  cudaStream_t, long long *, const Residual &, int *);                            \
+  template void launch_scatter<T>(const Geometry &, T *, const double *, int, int, int, cudaStream_t, long long *,  \
+                                  __nv_bfloat16 *);                                                               \
+  template void launch_gather<T>(const Geometry &, double *, const T *, int, int, int, cudaStream_t, long long *,  \
+                                 const __nv_bfloat16 *);                                                          \
+  template void launch_set_exact<T>(const Geometry &, T *, int, int, double, cudaStream_t, long long *,            \
+                                    __nv_bfloat16 *);                                                             \
   template void launch_pressure_mean_diff<T>(const Geometry &, const T *, int, double, double *, cudaStream_t,     \
                                              long long *);                                                         \
   template void launch_add_scalar<T>(const Geometry &, T *, const double *, cudaStream_t, long long *);            \
   template void launch_velocity_errors<T>(const Geometry &, T *const[3], int, int, double, double *, cudaStream_t, \
-                                          long long *);                                                            \
+                                          long long *, const Residual &);                                          \
   template void launch_pressure_errors<T>(const Geometry &, const T *, int, double, double *, cudaStream_t,        \
                                           long long *);                                                            \
-  template void launch_pressure_gradient<T>(const Geometry &, T *const[3], const T *, cudaStream_t, long long *);  \
-  template void launch_nonfinite_check<T>(const T *, long, int *, cudaStream_t, long long *);
+  template void launch_pressure_gradient<T>(const Geometry &, T *const[3], const T *, cudaStream_t, long long *);
 
 }  // namespace mifgpu

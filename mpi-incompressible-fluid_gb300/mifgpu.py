@@ -23,8 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmifgpu.so")
 
 FIELDS = {"u": 0, "v": 1, "w": 2, "u1": 3, "v1": 4, "w1": 5, "u2": 6, "v2": 7, "w2": 8, "p": 9, "phi": 10}
-FP64, MIXED = 0, 1
-FIELD_ZERO, FIELD_SINCOS, FIELD_ETHIER = 0, 1, 2
+FP64, MIXED, MIXED_COMPENSATED = 0, 1, 2
+FIELD_ZERO, FIELD_SINCOS, FIELD_ETHIER, FIELD_CALLER = 0, 1, 2, 3
 FORCING_NONE, FORCING_VELOCITY, FORCING_NAVIER_STOKES, FORCING_TAYLOR_GREEN = 0, 1, 2, 3
 
 EXPORTED = [
@@ -35,7 +35,8 @@ EXPORTED = [
     "mifgpu_adjust_pressure", "mifgpu_error_norms", "mifgpu_profile_step", "mifgpu_launch_count",
     "mifgpu_device_bytes", "mifgpu_gradient_ke", "mifgpu_backward", "mifgpu_download_adjoint",
     "mifgpu_set_forcing_amplitude", "mifgpu_velocity_error_norms_noalloc", "mifgpu_write_vtk",
-    "mifgpu_write_dat", "mifgpu_write_vtk_full_mesh", "mifgpu_probe_fp64_fma",
+    "mifgpu_write_dat", "mifgpu_write_vtk_full_mesh", "mifgpu_probe_fp64_fma", "mifgpu_set_boundary_values",
+    "mifgpu_set_pressure_gradient_faces", "mifgpu_solve_pressure_nhn",
 ]
 PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
                    "x_inverse", "periodic", "project"]
@@ -105,6 +106,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_write_dat": [vp, C.c_char_p, i, d, d, d],
         "mifgpu_write_vtk_full_mesh": [vp, C.c_char_p],
         "mifgpu_probe_fp64_fma": [dp],
+        "mifgpu_set_boundary_values": [vp, i, dp, dp, dp],
+        "mifgpu_set_pressure_gradient_faces": [vp, i, C.POINTER(C.c_void_p)],
+        "mifgpu_solve_pressure_nhn": [vp, i, d, C.POINTER(C.c_void_p)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -248,6 +252,51 @@ class Solver:
         self._check(self.lib.mifgpu_solve_pressure(self.h, vset, dt), "solve_pressure")
 
     solve_pressure = solve_pressure_equation_homogeneous_periodic
+
+    # -- caller boundary data (boundary_kind FIELD_CALLER) --
+    def set_boundary_values(self, slot: int, u: np.ndarray, v: np.ndarray, w: np.ndarray) -> None:
+        """The Dirichlet face planes of u, v, w (reference layout; only the
+        faces are read) for time slot `slot`: 0 for apply_bc, 1..3 for the
+        stage times of the next step."""
+        arrs = []
+        for n, a in zip(("u", "v", "w"), (u, v, w)):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != self.shape(n):
+                raise MifGpuError(f"boundary values {n}: shape {a.shape} != {self.shape(n)}")
+            arrs.append(a)
+        self._check(self.lib.mifgpu_set_boundary_values(self.h, int(slot), *(a.ctypes.data for a in arrs)),
+                    "set_boundary_values")
+
+    def face_shapes(self) -> list:
+        """Shapes of the six pressure-gradient face arrays (x_min, x_max,
+        y_min, y_max, z_min, z_max), numpy order (slow axis first)."""
+        ex, ey, ez = self.extent("p")
+        return [(ez, ey), (ez, ey), (ez, ex), (ez, ex), (ey, ex), (ey, ex)]
+
+    def _faces(self, faces):
+        arrs = []
+        for f, (a, shp) in enumerate(zip(faces, self.face_shapes())):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != shp:
+                raise MifGpuError(f"face {f}: shape {a.shape} != {shp}")
+            arrs.append(a)
+        ptrs = (C.c_void_p * 6)(*(a.ctypes.data for a in arrs))
+        return arrs, ptrs
+
+    def set_pressure_gradient_faces(self, slot: int, faces) -> None:
+        """Normal pressure-gradient data (grad p(t_{k-1}) - grad p(t_k)) of
+        stage `slot` of the next non-homogeneous Neumann step."""
+        arrs, ptrs = self._faces(faces)
+        self._check(self.lib.mifgpu_set_pressure_gradient_faces(self.h, int(slot), ptrs),
+                    "set_pressure_gradient_faces")
+
+    def solve_pressure_equation_non_homogeneous_neumann(self, vset: int, dt: float, faces) -> None:
+        """phi from div(set)/dt and the caller's normal pressure-gradient faces
+        (src/PressureEquation.cpp:276-286)."""
+        arrs, ptrs = self._faces(faces)
+        self._check(self.lib.mifgpu_solve_pressure_nhn(self.h, int(vset), float(dt), ptrs), "solve_pressure_nhn")
+
+    solve_pressure_nhn = solve_pressure_equation_non_homogeneous_neumann
 
     def divergence(self, vset: int, dt: float) -> None:
         self._check(self.lib.mifgpu_divergence(self.h, vset, dt), "divergence")

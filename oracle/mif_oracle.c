@@ -23,6 +23,12 @@ typedef struct {
 typedef struct {
   mif_oracle_params prm;
   int forcing;
+  /* Sensitivity probe (not reference behaviour): every forcing value is
+   * multiplied by 1 + forcing_noise * r, r in [-1, 1) a hash of the point,
+   * the component and forcing_seed. 0 (the default) leaves the restatement
+   * bit-identical to the reference. */
+  double forcing_noise;
+  unsigned forcing_seed;
   /* src/Constants.cpp:58-94 with one rank. */
   double dt, h[3], o2h[3], o8h[3], oh2Re[3], h_2[3], oh[3];
   long E[3];    /* Nx, Ny, Nz */
@@ -127,6 +133,24 @@ int mif_oracle_set_forcing(void *h, int forcing) {
   return 0;
 }
 
+int mif_oracle_set_forcing_noise(void *h, double rel, unsigned seed) {
+  ((St *)h)->forcing_noise = rel;
+  ((St *)h)->forcing_seed = seed;
+  return 0;
+}
+
+/* r in [-1, 1) from a 32-bit integer hash (lowbias32) of point, component, seed. */
+static double probe_noise(const St *s, int c, long i, long j, long k) {
+  unsigned x = (unsigned)(i + s->Es[0] * (j + s->Es[1] * k)) * 3u + (unsigned)c;
+  x ^= s->forcing_seed * 0x9e3779b9u;
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return (double)x / 2147483648.0 - 1.0;
+}
+
 int mif_oracle_extent(void *h, int id, long out[3]) {
   fld *f = field((St *)h, id);
   if (!f) return -1;
@@ -220,7 +244,9 @@ static inline double rhs(const St *s, int c, fld *const V[3], long i, long j, lo
     const double x = c == 0 ? face(s, 0, i) : node(s, 0, i);
     const double y = c == 1 ? face(s, 1, j) : node(s, 1, j);
     const double z = c == 2 ? face(s, 2, k) : node(s, 2, k);
-    r = r + mf_forcing(s->prm.exact_kind, c, t, x, y, z, s->prm.Re, s->forcing == 2);
+    double f = mf_forcing(s->prm.exact_kind, c, t, x, y, z, s->prm.Re, s->forcing == 2);
+    if (s->forcing_noise != 0.0) f = f * (1.0 + s->forcing_noise * probe_noise(s, c, i, j, k));
+    r = r + f;
   }
   return r;
 }

@@ -38,6 +38,9 @@ typedef struct {
 void *mif_oracle_create(const mif_oracle_params *p);
 void mif_oracle_destroy(void *h);
 int mif_oracle_set_forcing(void *h, int forcing); /* 0 none, 1 velocity forcing, 2 with grad p */
+/* Sensitivity probe, not reference behaviour: scales each forcing value by
+ * 1 + rel * r with r in [-1, 1) hashed from the point and `seed` (0: off). */
+int mif_oracle_set_forcing_noise(void *h, double rel, unsigned seed);
 int mif_oracle_extent(void *h, int id, long out[3]);
 int mif_oracle_set(void *h, int id, const double *data);
 int mif_oracle_get(void *h, int id, double *data);

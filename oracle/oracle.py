@@ -24,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "libmifref.so")
 ORACLE_LIB = os.path.join(HERE, "libmif_oracle.so")
+ORACLE_FAST_LIB = os.path.join(HERE, "libmif_oracle_fast.so")
 
 FIELD_NAMES = ["u", "v", "w", "u1", "v1", "w1", "u2", "v2", "w2", "p", "phi"]
 FIELD_ID = {n: i for i, n in enumerate(FIELD_NAMES)}
@@ -245,9 +246,69 @@ class OracleSolver(_Solver):
         self._fn("set_forcing").argtypes = [C.c_void_p, C.c_int]
         self._fn("set_forcing")(self.h, int(case.forcing))
 
+    def set_forcing_noise(self, rel: float, seed: int = 1) -> None:
+        """Sensitivity probe (not reference behaviour): every forcing value is
+        scaled by 1 + rel * r, r in [-1, 1) hashed per point from `seed`;
+        rel = 0 restores the reference's arithmetic."""
+        fn = self._fn("set_forcing_noise")
+        fn.argtypes = [C.c_void_p, C.c_double, C.c_uint]
+        fn(self.h, float(rel), int(seed))
+
     @staticmethod
     def available() -> bool:
         return os.path.exists(ORACLE_LIB)
+
+
+class OracleFastSolver(OracleSolver):
+    """The same restatement built with the reference's optimisation flags
+    (oracle/libmif_oracle_fast.so): the CPU baseline's timing build only, never
+    a checker."""
+
+    lib_path = ORACLE_FAST_LIB
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(ORACLE_FAST_LIB)
+
+
+def pressure_gradient_value(kind: int, comp: int, t: float, x: float, y: float, z: float, Re: float) -> float:
+    """Component `comp` of the analytic family's pressure gradient at (t, x,
+    y, z) (oracle/manufactured.h, the functions the reference build uses)."""
+    lib = _load(ORACLE_LIB)
+    fn = lib.mif_oracle_pressure_gradient_value
+    fn.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+    fn.restype = C.c_double
+    return fn(int(kind), int(comp), float(t), float(x), float(y), float(z), float(Re))
+
+
+def gradient_faces(case: Case, t_new: float, t_old: float) -> list:
+    """The data apply_non_homogeneous_neumann adds (src/PressureEquation.cpp:10-56)
+    for the family's gradient difference over time, get_difference_over_time(t_new,
+    t_old) = grad p(t_old) - grad p(t_new): its normal component at the pressure
+    nodes of the faces x_min, x_max, y_min, y_max, z_min, z_max, each of numpy
+    shape (slow axis, fast axis) = the face's two other axes in reverse order."""
+    E = case.extents("p")
+    h = [case.size[d] / (case.n_global[d] - 1) for d in range(3)]
+    base = [-1 if case.periodic[d] else 0 for d in range(3)]
+
+    def pos(d, i):  # include/StaggeredTensor.h:113-119
+        return case.origin[d] + h[d] * (base[d] + i)
+
+    faces = []
+    for d in range(3):
+        a, b = (1, 2) if d == 0 else ((0, 2) if d == 1 else (0, 1))
+        for side in (0, 1):
+            arr = np.empty((E[b], E[a]))
+            for pb in range(E[b]):
+                for pa in range(E[a]):
+                    idx = [0, 0, 0]
+                    idx[d] = 0 if side == 0 else E[d] - 1
+                    idx[a], idx[b] = pa, pb
+                    x, y, z = (pos(q, idx[q]) for q in range(3))
+                    arr[pb, pa] = (pressure_gradient_value(case.exact_kind, d, t_old, x, y, z, case.Re) -
+                                   pressure_gradient_value(case.exact_kind, d, t_new, x, y, z, case.Re))
+            faces.append(arr)
+    return faces
 
 
 def r2r(kind: int, x: np.ndarray, direct: bool = False) -> np.ndarray:
@@ -263,11 +324,25 @@ def r2r(kind: int, x: np.ndarray, direct: bool = False) -> np.ndarray:
     return out
 
 
-def build(ref_dir: str | None = None, with_ref: bool = True) -> None:
-    """Compile the restatement and, when the reference sources exist, the reference library."""
+def reference_dir(ref_dir: str | None = None) -> str | None:
+    """Where the reference's sources are: `ref_dir`, else MIF_REFERENCE_DIR,
+    else a `reference` checkout beside this repository; None if none exists."""
+    cands = [ref_dir, os.environ.get("MIF_REFERENCE_DIR"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "src")):
+            return c
+    return None
+
+
+def build(ref_dir: str | None = None, with_ref: bool = True, fast: bool = False) -> None:
+    """Compile the restatement (and its timing build when `fast`) and, when
+    the reference sources exist, the reference library."""
     import subprocess
 
     subprocess.run(["make", "-s", "-C", HERE, "libmif_oracle.so"], check=True)
-    ref = ref_dir or os.environ.get("MIF_REFERENCE_DIR", "/root/reference")
-    if with_ref and os.path.isdir(os.path.join(ref, "src")):
+    if fast:
+        subprocess.run(["make", "-s", "-C", HERE, "libmif_oracle_fast.so"], check=True)
+    ref = reference_dir(ref_dir)
+    if with_ref and ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)

@@ -23,6 +23,9 @@ int main() {
   s.timestep_velocity(0.0);
   s.solve_pressure_equation_homogeneous_periodic(0, 1.0);
   s.apply_bc(0, 0.0);
+  s.set_boundary_values(1, b, b, b);
+  s.set_pressure_gradient_faces(1, {b, b, b, b, b, b});
+  s.solve_pressure_equation_non_homogeneous_neumann(0, 1.0, {b, b, b, b, b, b});
   s.adjust_pressure(0.0);
   s.error_norms(0.0);
   s.set_exact_velocity(0, 0.0);

@@ -5,6 +5,7 @@ are ragged on purpose (no two axes equal, odd and even point counts) and
 cover every boundary combination the reference supports on one rank.
 """
 TWO_PI = 6.283185307179586
+HALF_PI = 1.5707963267948966
 
 CASES = {
     # test/full_test.cpp set-up: Ethier-Steinman exact solution, all Dirichlet.
@@ -45,6 +46,13 @@ CASES = {
     "poisson_periodic_odd": dict(
         case=dict(n_global=(8, 10, 12), size=(TWO_PI, TWO_PI, TWO_PI), Re=1.0, dt=1.0, periodic=(True, True, True)),
         init="random", seed=9, op="solve_pressure", solve_dt=0.5),
+    # Stand-alone non-homogeneous Neumann solve on the test/pressure_test_nhn.cpp
+    # shape (N x 3N x 5N on [-pi/2, 0]^3, dt = 1): random velocity, boundary
+    # data = grad p(t_old) - grad p(t_new) of the Ethier-Steinman pressure.
+    "poisson_nhn": dict(
+        case=dict(n_global=(4, 12, 20), size=(HALF_PI, HALF_PI, HALF_PI), origin=(-HALF_PI, -HALF_PI, -HALF_PI),
+                  Re=1.0, dt=1.0, exact_kind=2),
+        init="random", seed=21, op="solve_pressure_nhn", solve_dt=1.0, t_new=0.3, t_old=0.2),
     # Boundary fill alone.
     "bc_ethier": dict(
         case=dict(n_global=(6, 7, 8), size=(1.0, 1.0, 2.0), origin=(0.0, 0.0, -1.0), Re=1e3, dt=1e-4,

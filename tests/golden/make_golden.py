@@ -50,6 +50,8 @@ def run_case(name, spec):
             ref.solve_pressure(0, spec.get("solve_dt", 1.0))
         elif op == "apply_bc":
             ref.apply_bc(0, spec.get("bc_t", 0.3))
+        elif op == "solve_pressure_nhn":
+            ref.solve_pressure_nhn(0, spec.get("solve_dt", 1.0), spec["t_new"], spec["t_old"])
         else:
             raise ValueError(op)
     outputs = {n: ref.get(n) for n in O.FIELD_NAMES}

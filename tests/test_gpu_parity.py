@@ -57,6 +57,11 @@ def run_op(s, spec, dt):
         op = spec["op"]
         if op == "solve_pressure":
             s.solve_pressure(0, spec.get("solve_dt", 1.0))
+        elif op == "solve_pressure_nhn":
+            import oracle as O
+
+            faces = O.gradient_faces(O.Case(**spec["case"]), spec["t_new"], spec["t_old"])
+            s.solve_pressure_nhn(0, spec.get("solve_dt", 1.0), faces)
         elif op == "apply_bc":
             s.apply_bc(0, spec.get("bc_t", 0.3))
         else:
@@ -333,3 +338,30 @@ def test_mixed_poisson_matches_oracle(oracle_lib, mifgpu_lib, cuda_device, shape
     g.solve_pressure(0, 0.5)
     want = o.get("phi")
     assert rel_err(g.download("phi"), want) <= 2e-5
+
+
+def test_nonfinite_watchdog(mifgpu_lib, cuda_device):
+    """A NaN placed in the velocity from the host reaches every value of the
+    pressure increment; the step reports MIFGPU_ENONFINITE (-5), also through
+    the drop-in host call, and a clean state steps normally again."""
+    mg = mifgpu_lib
+    for prec in (mg.FP64, mg.MIXED, mg.MIXED_COMPENSATED):
+        g = make_solver(mg, dict(n_global=(17, 18, 19), exact_kind=2), precision=prec)
+        g.set_exact_velocity(0, 0.0)
+        g.set_exact_pressure(0.0)
+        g.run(0.0, 1)
+        clean = {n: g.download(n) for n in ("u", "v", "w", "p")}
+        bad = clean["v"].copy()
+        bad[5, 6, 7] = np.nan
+        g.upload("v", bad)
+        with pytest.raises(mg.MifGpuError, match=r"\(-5\).*NaN or Inf"):
+            g.run(1e-4, 2)
+        arrs = [clean[n].copy() for n in ("u", "v", "w", "p")]  # timestep_host writes into them
+        arrs[2][3, 3, 3] = np.inf
+        with pytest.raises(mg.MifGpuError, match=r"\(-5\)"):
+            g.timestep_host(1e-4, *arrs)
+        assert not np.isfinite(arrs[0]).all()  # the non-finite state came back to the host
+        g.load_state(clean)
+        g.run(1e-4, 2)
+        assert all(np.isfinite(g.download(n)).all() for n in ("u", "v", "w", "p"))
+        g.close()

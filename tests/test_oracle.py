@@ -88,6 +88,8 @@ def _run_oracle(oracle_lib, spec, fixture):
             s.solve_pressure(0, spec.get("solve_dt", 1.0))
         elif op == "apply_bc":
             s.apply_bc(0, spec.get("bc_t", 0.3))
+        elif op == "solve_pressure_nhn":
+            s.solve_pressure_nhn(0, spec.get("solve_dt", 1.0), spec["t_new"], spec["t_old"])
         else:
             getattr(s, op)(t)
     return s, case

@@ -13,10 +13,15 @@ def make(mg, n_global, precision, periodic=(False, False, False), kind=1):
                      boundary_kind=kind, forcing=mg.FORCING_NAVIER_STOKES)
 
 
-@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
-def test_noalloc_norms_match_error_norms(mifgpu_lib, cuda_device, precision):
+@pytest.mark.parametrize("precision", [0, 1, 2], ids=["fp64", "mixed", "compensated"])
+@pytest.mark.parametrize("periodic,kind", [((False, False, False), 1), ((True, False, True), 2)],
+                         ids=["dirichlet", "periodic_xz"])
+def test_noalloc_norms_match_error_norms(mifgpu_lib, cuda_device, precision, periodic, kind):
+    """Dirichlet box with the SINCOS family, and a box periodic in x and z
+    (interior index ranges shifted by the ghosts) with the Ethier-Steinman
+    family; every precision, the compensated one reading hi + residual."""
     mg = mifgpu_lib
-    s = make(mg, (17, 18, 19), precision)
+    s = make(mg, (17, 18, 19), precision, periodic=periodic, kind=kind)
     s.set_exact_velocity(0, 0.3)
     s.set_exact_pressure(0.3)
     rng = np.random.default_rng(2)
@@ -28,8 +33,10 @@ def test_noalloc_norms_match_error_norms(mifgpu_lib, cuda_device, precision):
     first = s.velocity_error_norms_noalloc(t)
     second = s.velocity_error_norms_noalloc(t)
     np.testing.assert_array_equal(first, second)  # fixed reduction order
+    # the two entry points' per-point arithmetic is compiled separately (its
+    # multiply-adds may contract differently), so even the maximum agrees to
+    # rounding, not bit for bit
     np.testing.assert_allclose(first, want, rtol=1e-12, atol=0)
-    assert first[2] == want[2]  # the maximum does not depend on the order
     s.close()
 
 
