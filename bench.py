@@ -20,7 +20,9 @@ L-infinity velocity error against the exact solution over FP64's (the
 Extra modes (each prints one JSON line): --configs runs the reference's
 benchmark configurations 1-3 at their sizes; --sweep runs the Ethier-Steinman
 refinement 32^3 -> 768^3 in FP64 and both float modes (convergence order and
-matched error); --adjoint-only runs the adjoint workload alone.
+matched error); --velocity runs the reference's own benchmark harness (the
+velocity-only step, N = 32..512); --adjoint-only runs the adjoint workload
+alone.
 
 Arms:
   --impl gb300      (default) the CUDA library: `value` from CUDA events around
@@ -685,6 +687,57 @@ def sweep(stream, sizes=(32, 64, 128, 256, 512, 768)):
     return {"case": "Ethier-Steinman on [0,1]^3, Re=1000, T=1e-4 in 2 steps (test/full_test.cpp)", "rows": rows}
 
 
+def velocity_benchmark(stream, sizes=(32, 64, 128, 256, 512), steps=20):
+    """The reference's own benchmark harness (test/benchmark.cpp:26-61): the
+    velocity-only RK3 step (mif::timestep_velocity) on the unit cube with N
+    points per axis, N = 32..512, Re = 1e6, dt = 1e-4, the SINCOS velocity
+    with its forcing; its counter is seconds per DoF (N^3) per step. Here:
+    graph-replayed steps (mifgpu_run_velocity) timed with CUDA events after
+    3 warm-up steps, FP64 and float, and the oracle's timestep_velocity on one
+    core (timing build) at the two smallest sizes for comparison."""
+    import torch
+
+    import mifgpu
+    import oracle as O
+
+    rows = []
+    for n in sizes:
+        row = {"N": n, "dof": n ** 3}
+        for pname, prec in (("fp64", mifgpu.FP64), ("mixed", mifgpu.MIXED)):
+            s = mifgpu.Solver(n_global=(n, n, n), Re=1e6, dt=1e-4, precision=prec, boundary_kind=mifgpu.FIELD_SINCOS,
+                              forcing=mifgpu.FORCING_VELOCITY)
+            s.set_stream(stream.cuda_stream)
+            s.set_exact_velocity(0, 0.0)
+            s.run_velocity(0.0, 3)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.run_velocity(3e-4, steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            row[pname] = {"ms_per_step": round(ms, 5), "ns_per_dof_step": ms * 1e6 / n ** 3,
+                          "gdof_steps_s": n ** 3 / ms / 1e6}
+            s.close()
+            torch.cuda.empty_cache()
+        rows.append(row)
+    O.build(with_ref=False, fast=True)
+    cpu = []
+    for n in sizes[:2]:
+        case = O.Case(n_global=(n, n, n), Re=1e6, dt=1e-4, exact_kind=O.KIND_SINCOS)
+        o = O.OracleFastSolver(case)
+        o.set_exact_velocity(0, 0.0, True)
+        o.timestep_velocity(0.0)
+        t0 = time.perf_counter()
+        for k in range(3):
+            o.timestep_velocity((1 + k) * 1e-4)
+        el = (time.perf_counter() - t0) / 3
+        cpu.append({"N": n, "ms_per_step": round(el * 1e3, 3), "ns_per_dof_step": el * 1e9 / n ** 3,
+                    "cores": 1, "build": CPU_FLAGS})
+    return {"case": "test/benchmark.cpp: velocity-only RK3 step, unit cube, Re=1e6, dt=1e-4, SINCOS velocity "
+                    "with forcing", "rows": rows, "cpu_oracle": cpu}
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def workload_cells(workload: str) -> int:
@@ -966,6 +1019,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--configs", action="store_true", help="the reference's configurations 1-3 (one JSON line)")
     ap.add_argument("--sweep", action="store_true", help="Ethier-Steinman refinement 32^3..768^3 (one JSON line)")
+    ap.add_argument("--velocity", action="store_true",
+                    help="the reference's velocity-only benchmark, N = 32..512 (one JSON line)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="only the adjoint workload (a profiling aid; prints {'adjoint': ...})")
     args = ap.parse_args()
@@ -973,14 +1028,19 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif args.configs or args.sweep:
+    elif args.configs or args.sweep or args.velocity:
         import torch
 
         import build as pkg_build
 
         pkg_build.build()
         stream = torch.cuda.Stream()
-        print(json.dumps({"configs": config_suite(stream)} if args.configs else {"sweep": sweep(stream)}))
+        if args.configs:
+            print(json.dumps({"configs": config_suite(stream)}))
+        elif args.sweep:
+            print(json.dumps({"sweep": sweep(stream)}))
+        else:
+            print(json.dumps({"velocity_benchmark": velocity_benchmark(stream)}))
     elif args.adjoint_only:
         import torch
 

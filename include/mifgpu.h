@@ -179,6 +179,12 @@ int mifgpu_timestep_nhn(mifgpu_ctx *ctx, double t_n);
  * src/TimestepVelocity.cpp:89. */
 int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n);
 
+/* `nsteps` velocity-only steps from t0 with t_n = t0 + n*dt, each ending with
+ * the swap, replayed from the captured graphs of the two labellings with no
+ * host synchronisation between steps: the loop of the reference's benchmark
+ * harness over mif::timestep_velocity (test/benchmark.cpp:42-50). */
+int mifgpu_run_velocity(mifgpu_ctx *ctx, double t0, int nsteps);
+
 /* Sub-steps, for parity testing and for callers that assemble their own step:
  *   apply_bc       VelocityTensor::apply_bc on set `set` at time t
  *                  (src/VelocityTensor.cpp:36-233)

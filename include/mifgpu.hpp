@@ -93,6 +93,7 @@ class Solver {
   void run(double t0, int nsteps) { check(mifgpu_run(ctx_, t0, nsteps), "run"); }
   void timestep_nhn(double t_n) { check(mifgpu_timestep_nhn(ctx_, t_n), "timestep_nhn"); }
   void timestep_velocity(double t_n) { check(mifgpu_timestep_velocity(ctx_, t_n), "timestep_velocity"); }
+  void run_velocity(double t0, int nsteps) { check(mifgpu_run_velocity(ctx_, t0, nsteps), "run_velocity"); }
   void solve_pressure_equation_homogeneous_periodic(int velocity_set, double dt) {
     check(mifgpu_solve_pressure(ctx_, velocity_set, dt), "solve_pressure");
   }

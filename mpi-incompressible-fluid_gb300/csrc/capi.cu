@@ -658,8 +658,18 @@ struct Impl final : ImplBase {
     return MIFGPU_OK;
   }
 
+  // `nsteps` replays of the step graph of `variant`. The velocity-only step
+  // ends with the swap of sets 0 and 1 (src/TimestepVelocity.cpp:89), a
+  // relabelling: its replays alternate the graphs of the two labellings.
   int step(mifgpu_ctx *ctx, int variant, const double *host_slots, int nsteps) override {
+    const bool swap = variant == kVariantVelocity;
     if (int rc = ensure_graph(ctx, variant)) return rc;
+    if (swap && nsteps > 1) {
+      swap_sets();
+      const int rc = ensure_graph(ctx, variant);
+      swap_sets();
+      if (rc) return rc;
+    }
     CK(cudaMemsetAsync(nonfinite, 0, sizeof(int), ctx->stream));
     for (int n0 = 0; n0 < nsteps; n0 += slots_cap) {
       const int chunk = std::min(slots_cap, nsteps - n0);
@@ -669,6 +679,7 @@ struct Impl final : ImplBase {
       for (int n = 0; n < chunk; ++n) {
         CK(cudaGraphLaunch(graph[variant][parity], ctx->stream));
         ctx->launches += graph_launches[variant][parity];
+        if (swap) swap_sets();
       }
     }
     // The host copy of the slots may be a temporary: wait until it was consumed.
@@ -1214,9 +1225,21 @@ int mifgpu_timestep_velocity(mifgpu_ctx *ctx, double t_n) {
     return fail(ctx, MIFGPU_ENOTSUP, "the velocity-only step runs in MIFGPU_FP64 or MIFGPU_MIXED");
   double s[kSlotSize];
   velocity_slot(t_n, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s);
-  if (int rc = ctx->impl->step(ctx, kVariantVelocity, s, 1)) return rc;
-  ctx->impl->swap_sets();  // src/TimestepVelocity.cpp:89
-  return MIFGPU_OK;
+  return ctx->impl->step(ctx, kVariantVelocity, s, 1);  // ends with the swap, src/TimestepVelocity.cpp:89
+}
+
+int mifgpu_run_velocity(mifgpu_ctx *ctx, double t0, int nsteps) {
+  if (!ctx || nsteps < 0) return MIFGPU_EINVAL;
+  if (nsteps == 0) return MIFGPU_OK;
+  if (ctx->prm.precision == MIFGPU_MIXED_COMPENSATED)
+    return fail(ctx, MIFGPU_ENOTSUP, "the velocity-only step runs in MIFGPU_FP64 or MIFGPU_MIXED");
+  if (nsteps > 1 && ctx->prm.boundary_kind == MIFGPU_FIELD_CALLER)
+    return fail(ctx, MIFGPU_ENOTSUP,
+                "with boundary_kind MIFGPU_FIELD_CALLER the boundary data is set per step: run one step at a time");
+  std::vector<double> s((size_t)kSlotSize * nsteps);
+  for (int n = 0; n < nsteps; ++n)
+    velocity_slot(t0 + n * ctx->g.dt, ctx->g.dt, ctx->prm.boundary_kind, ctx->g.Re, s.data() + (size_t)kSlotSize * n);
+  return ctx->impl->step(ctx, kVariantVelocity, s.data(), nsteps);
 }
 
 int mifgpu_set_boundary_values(mifgpu_ctx *ctx, int slot, const double *u, const double *v, const double *w) {

@@ -36,7 +36,7 @@ EXPORTED = [
     "mifgpu_device_bytes", "mifgpu_gradient_ke", "mifgpu_backward", "mifgpu_download_adjoint",
     "mifgpu_set_forcing_amplitude", "mifgpu_velocity_error_norms_noalloc", "mifgpu_write_vtk",
     "mifgpu_write_dat", "mifgpu_write_vtk_full_mesh", "mifgpu_probe_fp64_fma", "mifgpu_set_boundary_values",
-    "mifgpu_set_pressure_gradient_faces", "mifgpu_solve_pressure_nhn",
+    "mifgpu_set_pressure_gradient_faces", "mifgpu_solve_pressure_nhn", "mifgpu_run_velocity",
 ]
 PROFILE_CLASSES = ["stage", "boundary", "divergence", "x_forward", "y_forward", "z_fused", "y_inverse",
                    "x_inverse", "periodic", "project"]
@@ -88,6 +88,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mifgpu_timestep_host": [vp, d, dp, dp, dp, dp],
         "mifgpu_timestep_nhn": [vp, d],
         "mifgpu_timestep_velocity": [vp, d],
+        "mifgpu_run_velocity": [vp, d, i],
         "mifgpu_apply_bc": [vp, i, d],
         "mifgpu_solve_pressure": [vp, i, d],
         "mifgpu_divergence": [vp, i, d],
@@ -244,6 +245,10 @@ class Solver:
 
     def timestep_velocity(self, t_n: float) -> None:
         self._check(self.lib.mifgpu_timestep_velocity(self.h, t_n), "timestep_velocity")
+
+    def run_velocity(self, t0: float, nsteps: int) -> None:
+        """`nsteps` velocity-only steps from graph replays (test/benchmark.cpp's loop)."""
+        self._check(self.lib.mifgpu_run_velocity(self.h, t0, int(nsteps)), "run_velocity")
 
     def apply_bc(self, vset: int, t: float) -> None:
         self._check(self.lib.mifgpu_apply_bc(self.h, vset, t), "apply_bc")

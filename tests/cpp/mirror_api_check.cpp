@@ -21,6 +21,7 @@ int main() {
   s.run(0.0, 1);
   s.timestep_nhn(0.0);
   s.timestep_velocity(0.0);
+  s.run_velocity(0.0, 2);
   s.solve_pressure_equation_homogeneous_periodic(0, 1.0);
   s.apply_bc(0, 0.0);
   s.set_boundary_values(1, b, b, b);
