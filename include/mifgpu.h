@@ -296,8 +296,14 @@ int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIF
  * every point of their extents, ghosts included) and 9 (pressure).
  * `dloss_dalpha` (may be null) receives the derivative with respect to
  * forcing_amplitude when the forcing is MIFGPU_FORCING_TAYLOR_GREEN, else 0.
- * `ms_out` (may be null) receives milliseconds of the forward pass, the
- * segment recomputes and the reverse sweeps, timed with CUDA events. */
+ * The backward pass recomputes each segment on a second stream into one of
+ * two snapshot buffers, so the recompute of a segment runs beside the reverse
+ * sweep of the one after it (with one buffer, when two do not fit, they
+ * alternate). `ms_out` (may be null) receives milliseconds, timed with CUDA
+ * events: [0] the forward pass, [1] the whole backward pass (seed,
+ * recomputes and reverse sweeps, wall time), [2] the reverse sweeps alone
+ * (summed over the segments on the reverse stream; they share the GPU with
+ * the recomputes beside them). */
 
 /* Loss = 1/2 hx hy hz * sum of u_c^2 over the interior staggered points of
  * each component whose position lies in box = {x0, x1, y0, y1, z0, z1}

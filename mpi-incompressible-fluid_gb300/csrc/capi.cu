@@ -226,6 +226,10 @@ struct Impl final : ImplBase {
   // One captured reverse step per snapshot slot (the slot's address is baked in).
   std::vector<cudaGraphExec_t> rev_graph;
   long long rev_graph_launches = 0;
+  // The backward pass's second stream (segment recomputes) and the events
+  // that hand each of the two snapshot buffers between the streams.
+  cudaStream_t rec_stream = nullptr;
+  cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
 
   void mark(int cls, cudaStream_t s) {
     if (!prof) return;
@@ -258,6 +262,11 @@ struct Impl final : ImplBase {
     for (auto &gx : rev_graph)
       if (gx) cudaGraphExecDestroy(gx);
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (rec_stream) cudaStreamDestroy(rec_stream);
+    for (int b = 0; b < 2; ++b) {
+      if (ev_rec[b]) cudaEventDestroy(ev_rec[b]);
+      if (ev_rev[b]) cudaEventDestroy(ev_rev[b]);
+    }
     for (int q = 1; q < kXferSlots; ++q) cudaFree(xfer[q]);
     for (auto &row : xfer_ev)
       for (auto &e : row)
@@ -892,53 +901,73 @@ struct Impl final : ImplBase {
       CK(AdjointOps<T>::prepare());
     }
     if (int rc = ensure_fields(ctx, ckpt_block, ckpt_fields, (size_t)4 * (nseg + 1), "checkpoints")) return rc;
+    // Two snapshot buffers of 9 C fields, so that one segment's recompute
+    // can run beside the previous segment's reverse sweep; one if two do not
+    // fit (then the two alternate on the GPU).
     T *const snap_before = snap_block;
-    if (int rc = ensure_fields(ctx, snap_block, snap_fields, (size_t)9 * C, "segment snapshots")) return rc;
+    if (snap_fields < (size_t)18 * C && ensure_fields(ctx, snap_block, snap_fields, (size_t)18 * C, "segment snapshots")) {
+      cudaGetLastError();
+      if (int rc = ensure_fields(ctx, snap_block, snap_fields, (size_t)9 * C, "segment snapshots")) return rc;
+    }
     if (snap_block != snap_before) drop_rev_graphs();
+    const int nbuf = snap_fields >= (size_t)18 * C ? 2 : 1;
+    if (!rec_stream) CK(cudaStreamCreateWithFlags(&rec_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+      if (!ev_rec[b]) CK(cudaEventCreateWithFlags(&ev_rec[b], cudaEventDisableTiming));
+      if (!ev_rev[b]) CK(cudaEventCreateWithFlags(&ev_rev[b], cudaEventDisableTiming));
+    }
     if (int rc = ensure_graph(ctx, kVariantProjection)) return rc;
-    cudaStream_t s = ctx->stream;
+    cudaStream_t s = ctx->stream, r = rec_stream;
     long long *cnt = &ctx->launches;
     std::vector<double> sl((size_t)kSlotSize * N);
     for (int n = 0; n < N; ++n)
       projection_slot(req.t0 + n * g.dt, g.dt, ctx->prm.boundary_kind, g.Re, sl.data() + (size_t)kSlotSize * n);
     T *set0 = F.vel(0, 0), *set1 = F.vel(1, 0), *set2 = F.vel(2, 0), *p = F.f[kP];
     auto ck = [&](int seg) { return ckpt_block + (size_t)4 * seg * field_elems; };
-    auto sn = [&](int m) { return snap_block + (size_t)9 * m * field_elems; };
-    std::vector<std::pair<int, cudaEvent_t>> marks;
-    auto phase = [&](int ph) {
+    // snapshot slot q = b C + m: step m of a segment in buffer b
+    auto sn = [&](int q) { return snap_block + (size_t)9 * q * field_elems; };
+    // timing events: forward start / end, backward end, and per segment the
+    // start and end of its reverse sweep on the reverse stream
+    std::vector<cudaEvent_t> evs;
+    auto stamp = [&](cudaStream_t st) {
       cudaEvent_t e;
       cudaEventCreate(&e);
-      cudaEventRecord(e, s);
-      marks.push_back({ph, e});
+      cudaEventRecord(e, st);
+      evs.push_back(e);
+      return e;
     };
     auto cleanup = [&]() {
-      for (auto &m : marks) cudaEventDestroy(m.second);
+      for (auto &e : evs) cudaEventDestroy(e);
     };
-    auto run_seg = [&](int seg, bool snap) -> cudaError_t {
+    // the steps of segment seg from its checkpointed start on stream st; with
+    // snapshots into buffer b, the three sets each stage's right-hand side
+    // is evaluated at
+    auto run_seg = [&](int seg, int b, cudaStream_t st) -> cudaError_t {
       const int n0 = seg * C, len = std::min(C, N - n0);
       cudaError_t e = cudaMemcpyAsync(slots, sl.data() + (size_t)kSlotSize * n0, sizeof(double) * kSlotSize * len,
-                                      cudaMemcpyHostToDevice, s);
-      if (e == cudaSuccess) e = cudaMemsetAsync(step_ctr, 0, sizeof(int), s);
+                                      cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(step_ctr, 0, sizeof(int), st);
       for (int m = 0; m < len && e == cudaSuccess; ++m) {
-        if (snap) e = copy_fields(sn(m), set0, 3, s);
-        if (e == cudaSuccess) e = cudaGraphLaunch(graph[kVariantProjection][parity], s);
+        T *snap = b >= 0 ? sn(b * C + m) : nullptr;
+        if (snap) e = copy_fields(snap, set0, 3, st);
+        if (e == cudaSuccess) e = cudaGraphLaunch(graph[kVariantProjection][parity], st);
         *cnt += graph_launches[kVariantProjection][parity];
-        if (snap && e == cudaSuccess) e = copy_fields(sn(m) + 3 * field_elems, set1, 3, s);
-        if (snap && e == cudaSuccess) e = copy_fields(sn(m) + 6 * field_elems, set2, 3, s);
+        if (snap && e == cudaSuccess) e = copy_fields(snap + 3 * field_elems, set1, 3, st);
+        if (snap && e == cudaSuccess) e = copy_fields(snap + 6 * field_elems, set2, 3, st);
       }
       return e;
     };
     // forward pass, one checkpoint per segment start and one of the final state
-    phase(0);
+    cudaEvent_t t_fwd0 = stamp(s);
     for (int seg = 0; seg < nseg; ++seg) {
       cudaError_t e = copy_fields(ck(seg), set0, 3, s);
       if (e == cudaSuccess) e = copy_fields(ck(seg) + 3 * field_elems, p, 1, s);
-      if (e == cudaSuccess) e = run_seg(seg, false);
+      if (e == cudaSuccess) e = run_seg(seg, -1, s);
       if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "forward pass");
     }
     CK(copy_fields(ck(nseg), set0, 3, s));
     CK(copy_fields(ck(nseg) + 3 * field_elems, p, 1, s));
-    phase(2);
+    cudaEvent_t t_fwd1 = stamp(s);
     // seed the adjoint of the final state
     T *lx[3] = {adj_field(kLX), adj_field(kLX + 1), adj_field(kLX + 2)};
     CK(cudaMemsetAsync(acc, 0, sizeof(double) * 2, s));
@@ -961,25 +990,52 @@ struct Impl final : ImplBase {
         launch_scatter<T>(g, dst[q], staging, e3[0], e3[1], e3[2], s, cnt);
       }
     }
-    // backward: per segment, recompute it with snapshots, then reverse its steps
-    for (int seg = nseg - 1; seg >= 0; --seg) {
-      phase(1);
-      const int len = std::min(C, N - seg * C);
-      cudaError_t e = copy_fields(set0, ck(seg), 3, s);
-      if (e == cudaSuccess) e = copy_fields(p, ck(seg) + 3 * field_elems, 1, s);
-      if (e == cudaSuccess) e = run_seg(seg, true);
-      if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "segment recompute");
-      phase(2);
+    // the recompute stream starts once the seed has read the final state
+    CK(cudaStreamWaitEvent(r, stamp(s), 0));
+    // backward: per segment, recompute it with snapshots (stream r), then
+    // reverse its steps (stream s). A buffer passes from a reverse sweep to
+    // the next recompute into it through ev_rev, and back through ev_rec.
+    auto recompute = [&](int seg) -> int {
+      const int b = seg % nbuf;
+      CK(cudaStreamWaitEvent(r, ev_rev[b], 0));
+      cudaError_t e = copy_fields(set0, ck(seg), 3, r);
+      if (e == cudaSuccess) e = copy_fields(p, ck(seg) + 3 * field_elems, 1, r);
+      if (e == cudaSuccess) e = run_seg(seg, b, r);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "segment recompute");
+      CK(cudaEventRecord(ev_rec[b], r));
+      return MIFGPU_OK;
+    };
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sweeps;
+    auto reverse = [&](int seg) -> int {
+      const int b = seg % nbuf, len = std::min(C, N - seg * C);
+      CK(cudaStreamWaitEvent(s, ev_rec[b], 0));
+      cudaEvent_t e0 = stamp(s);
       for (int m = len - 1; m >= 0; --m) {
+        const int q = b * C + m;
         const T *V[3][3];
         for (int st = 0; st < 3; ++st)
-          for (int c = 0; c < 3; ++c) V[st][c] = sn(m) + (size_t)(3 * st + c) * field_elems;
-        if (int rc = ensure_rev_graph(ctx, m, V)) return cleanup(), rc;
-        CK(cudaGraphLaunch(rev_graph[m], s));
+          for (int c = 0; c < 3; ++c) V[st][c] = sn(q) + (size_t)(3 * st + c) * field_elems;
+        if (int rc = ensure_rev_graph(ctx, q, V)) return rc;
+        CK(cudaGraphLaunch(rev_graph[q], s));
         *cnt += rev_graph_launches;
       }
+      sweeps.push_back({e0, stamp(s)});
+      CK(cudaEventRecord(ev_rev[b], s));
+      return MIFGPU_OK;
+    };
+    if (int rc = recompute(nseg - 1)) return cleanup(), rc;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+      // with two buffers the next segment's recompute runs beside this sweep
+      if (nbuf == 2 && seg > 0)
+        if (int rc = recompute(seg - 1)) return cleanup(), rc;
+      if (int rc = reverse(seg)) return cleanup(), rc;
+      if (nbuf == 1 && seg > 0)
+        if (int rc = recompute(seg - 1)) return cleanup(), rc;
     }
-    phase(3);
+    // the reverse stream takes over the forward fields again
+    cudaEvent_t r_done = stamp(r);
+    CK(cudaStreamWaitEvent(s, r_done, 0));
+    cudaEvent_t t_bwd1 = stamp(s);
     // leave the context at the final state
     CK(copy_fields(set0, ck(nseg), 3, s));
     CK(copy_fields(p, ck(nseg) + 3 * field_elems, 1, s));
@@ -991,11 +1047,15 @@ struct Impl final : ImplBase {
     if (req.loss) *req.loss = h[0];
     if (req.dalpha) *req.dalpha = h[1];
     if (req.ms) {
-      for (int q = 0; q < 3; ++q) req.ms[q] = 0.0;
-      for (size_t q = 0; q + 1 < marks.size(); ++q) {
-        float t = 0.f;
-        cudaEventElapsedTime(&t, marks[q].second, marks[q + 1].second);
-        if (marks[q].first < 3) req.ms[marks[q].first] += t;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, t_fwd0, t_fwd1);
+      req.ms[0] = t;
+      cudaEventElapsedTime(&t, t_fwd1, t_bwd1);
+      req.ms[1] = t;
+      req.ms[2] = 0.0;
+      for (auto &sw : sweeps) {
+        cudaEventElapsedTime(&t, sw.first, sw.second);
+        req.ms[2] += t;
       }
     }
     cleanup();

@@ -243,6 +243,29 @@ struct Taps {
     w20 = A(2, 0, -1, 1), w5 = A(2, 0, 0, -1), w17 = A(2, 0, 1, 0), w15 = A(2, 1, 0, 0);
     if (with_p) p14 = A(3, 0, 0, 0), p13 = A(3, -1, 0, 0), p11 = A(3, 0, -1, 0), p5 = A(3, 0, 0, -1);
   }
+  // Only the taps component c's right-hand side and pressure gradient read
+  // (15 of the 31, plus two of p).
+  __device__ __forceinline__ void load_c(const Tap<T> &A, int c, bool with_p) {
+    if (c == 0) {
+      u13 = A(0, -1, 0, 0), u11 = A(0, 0, -1, 0), u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u23 = A(0, 0, 0, 1);
+      u17 = A(0, 0, 1, 0), u15 = A(0, 1, 0, 0);
+      v13 = A(1, -1, 0, 0), v16 = A(1, -1, 1, 0), v14 = A(1, 0, 0, 0), v17 = A(1, 0, 1, 0);
+      w13 = A(2, -1, 0, 0), w22 = A(2, -1, 0, 1), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1);
+      if (with_p) p14 = A(3, 0, 0, 0), p13 = A(3, -1, 0, 0);
+    } else if (c == 1) {
+      u14 = A(0, 0, 0, 0), u15 = A(0, 1, 0, 0), u12 = A(0, 1, -1, 0), u11 = A(0, 0, -1, 0);
+      v13 = A(1, -1, 0, 0), v14 = A(1, 0, 0, 0), v17 = A(1, 0, 1, 0), v11 = A(1, 0, -1, 0);
+      v5 = A(1, 0, 0, -1), v23 = A(1, 0, 0, 1), v15 = A(1, 1, 0, 0);
+      w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1), w11 = A(2, 0, -1, 0), w20 = A(2, 0, -1, 1);
+      if (with_p) p14 = A(3, 0, 0, 0), p11 = A(3, 0, -1, 0);
+    } else {
+      u5 = A(0, 0, 0, -1), u14 = A(0, 0, 0, 0), u15 = A(0, 1, 0, 0), u6 = A(0, 1, 0, -1);
+      v5 = A(1, 0, 0, -1), v14 = A(1, 0, 0, 0), v17 = A(1, 0, 1, 0), v8 = A(1, 0, 1, -1);
+      w13 = A(2, -1, 0, 0), w14 = A(2, 0, 0, 0), w23 = A(2, 0, 0, 1), w11 = A(2, 0, -1, 0);
+      w5 = A(2, 0, 0, -1), w17 = A(2, 0, 1, 0), w15 = A(2, 1, 0, 0);
+      if (with_p) p14 = A(3, 0, 0, 0), p5 = A(3, 0, 0, -1);
+    }
+  }
   __device__ __forceinline__ T self(int c) const { return c == 0 ? u14 : (c == 1 ? v14 : w14); }
   // p at the point minus p one step back along axis c
   __device__ __forceinline__ T dp(int c) const { return p14 - (c == 0 ? p13 : (c == 1 ? p11 : p5)); }
@@ -399,11 +422,14 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4)
     for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
     const long q = qij + (long)k * sz;
     const unsigned hq = std::is_same<T, float>::value ? sr_mix((unsigned)q ^ salt) : 0u;
-    Taps<T> tp;
-    tp.load(A, kUseP);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (!own_ij[c] || k >= klim[c]) continue;
+      // each component's taps are read right before its update: the global
+      // stores of the previous component keep the compiler from hoisting
+      // them, so at most one component's taps are live (no spills)
+      Taps<T> tp;
+      tp.load_c(A, c, kUseP);
       T r = rhs_taps(c, tp, co);
       if (forcing) r = r + fe.eval(c, fx, fy, fz);
       T gp = T(0);

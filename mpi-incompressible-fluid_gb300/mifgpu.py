@@ -351,8 +351,9 @@ class Solver:
         """Kinetic energy in `box` (x0, x1, y0, y1, z0, z1) after `nsteps` steps from the
         current state and its gradient; the state advances to the final time.
 
-        Returns loss, dloss_dalpha and the milliseconds of the forward pass, the
-        segment recomputes and the reverse sweeps; the gradients with respect to
+        Returns loss, dloss_dalpha and the milliseconds of the forward pass,
+        the whole backward pass (segment recomputes overlapped with reverse
+        sweeps) and the reverse sweeps alone; the gradients with respect to
         the initial u, v, w, p come from ``adjoint(name)``."""
         b = np.ascontiguousarray(box, dtype=np.float64)
         loss, da = C.c_double(), C.c_double()
@@ -360,7 +361,7 @@ class Solver:
         self._check(self.lib.mifgpu_gradient_ke(self.h, t0, int(nsteps), int(checkpoint_every), b.ctypes.data,
                                                 C.addressof(loss), C.addressof(da), ms.ctypes.data),
                     "gradient_ke")
-        return {"loss": loss.value, "dloss_dalpha": da.value, "forward_ms": ms[0], "recompute_ms": ms[1],
+        return {"loss": loss.value, "dloss_dalpha": da.value, "forward_ms": ms[0], "backward_ms": ms[1],
                 "reverse_ms": ms[2]}
 
     def backward(self, t0: float, nsteps: int, checkpoint_every: int, seeds: dict) -> dict:
@@ -381,7 +382,7 @@ class Solver:
         ms = np.zeros(3)
         self._check(self.lib.mifgpu_backward(self.h, t0, int(nsteps), int(checkpoint_every), *ptrs,
                                              C.addressof(da), ms.ctypes.data), "backward")
-        return {"dloss_dalpha": da.value, "forward_ms": ms[0], "recompute_ms": ms[1], "reverse_ms": ms[2]}
+        return {"dloss_dalpha": da.value, "forward_ms": ms[0], "backward_ms": ms[1], "reverse_ms": ms[2]}
 
     def adjoint(self, name: str) -> np.ndarray:
         """d loss / d (initial field) of the last gradient_ke / backward call (u, v, w or p)."""
