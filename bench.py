@@ -111,13 +111,15 @@ def step_sweeps(precision: str) -> float:
 
 
 # DRAM read + write bytes over algorithmic bytes, from ncu captures of the
-# stage kernels on the 256x256x512 profiling case and of the line sweeps on
-# the 512x256x256 one: applied to the full launch. (The fused z sweep's
-# figure includes its 1/lambda table, one more field-sized read.)
+# stage, divergence and projection kernels on the 256x256x512 profiling case
+# and of the line sweeps on the 512x256x256 one: applied to the full launch.
+# (The fused z sweep's figure includes its 1/lambda table, one more
+# field-sized read.)
 MEASURED_TRAFFIC_RATIO = {
     "mixed": {"stage": 1.06, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
               "x_inverse": 0.82},
-    "compensated": {"x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81, "x_inverse": 0.82},
+    "compensated": {"stage": 1.06, "divergence": 1.03, "project": 0.99, "x_forward": 0.82, "y_forward": 0.81,
+                    "z_fused": 1.37, "y_inverse": 0.81, "x_inverse": 0.82},
 }
 # FP64 operations of one FP64 step per cell (an FMA counted as two), from the
 # DFMA / DADD / DMUL instruction counters of an ncu capture of the

@@ -67,6 +67,12 @@ struct LineArgs {
   const typename Vec2<T>::type *dsc;  // register path, kind 2: (sin, cos)(pi j / N)
   int P, lg_lines;        // line pairs per CTA; log2(2P)
   int line_fast;          // 1: consecutive threads take consecutive lines (strided axes)
+  // Line enumeration along a: line g is (qa' = g % na_lines, qb = g / na_lines),
+  // at owner index qa = qa' - lead, empty outside [0, na). With pair8 (register
+  // path, strided axes with sa = 1), na_lines and lead make the two lines of
+  // every pair adjacent and 8-byte aligned in memory, so a pair moves as one
+  // 8-byte element; otherwise na_lines = na and lead = 0.
+  int na_lines, lead, pair8;
   int vec16;              // x lines, register path, half-length DCT-I: 0, or the row pitch (floats)
                           // of the 16-byte staging (every line starts 16-byte aligned and its row
                           // holds the n points rounded up to 4)
@@ -88,8 +94,8 @@ __device__ void fill_line_table(LineTable &t, const LineArgs<T> &a, long line0, 
   const int nl = 2 * a.P;
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
     const long gl = line0 + l;
-    if (gl < total) {
-      const long qa = gl % a.na, qb = gl / a.na;
+    const long qa = gl % a.na_lines - a.lead, qb = gl / a.na_lines;
+    if (gl < total && qa >= 0 && qa < a.na) {
       t.off[l] = a.base + qa * a.sa + qb * a.sb;
       t.eoff[l] = qa + (long)a.na * qb;  // (x, y) of a z line in the owner block
     } else {
@@ -225,7 +231,7 @@ __global__ void __launch_bounds__(kThreads) line_kernel(LineArgs<T> a) {
   T2 *s = reinterpret_cast<T2 *>(smem_raw);
   constexpr int MAXE = MaxE<T>::v;
   const int LS = a.L + 1;
-  const long total = (long)a.na * a.nb;
+  const long total = (long)a.na_lines * a.nb;
   const long line0 = (long)blockIdx.x * 2 * a.P;
   const bool pow2 = a.pow2 != 0;
 
@@ -271,6 +277,10 @@ __global__ void eigen_table_kernel(T *eig, const double *lx, const double *ly, c
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
 }
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -547,7 +557,7 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ LineTable table;
   T2 *s = reinterpret_cast<T2 *>(smem_raw);
-  const long total = (long)a.na * a.nb;
+  const long total = (long)a.na_lines * a.nb;
   const long line0 = (long)blockIdx.x * 2 * a.P;
   const int pp = threadIdx.x / N2, t = threadIdx.x % N2;
   T2 *row = s + pp * ROW;
@@ -560,7 +570,24 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   // x lines put a warp on one line. (Splitting a warp into two 16-line or
   // two-line halves makes the 4-byte shared-memory writes conflict free but
   // halves the segments, and ran slower.)
-  if (a.line_fast) {
+  if (a.line_fast && a.pair8) {
+    // pair p of the CTA is lines 2p, 2p+1, adjacent in memory from an even
+    // address: one 8-byte copy per point (16 pairs of a warp span 128 bytes)
+    const int p = threadIdx.x & (a.P - 1), ms = blockDim.x >> (a.lg_lines - 1);
+    const long offa = table.off[2 * p], offb = table.off[2 * p + 1];
+    T2 *dst = s + p * ROW;
+    if (offa >= 0 && offb >= 0) {
+      const T *src0 = a.data + offa;
+      for (int m = threadIdx.x >> (a.lg_lines - 1); m < n; m += ms) cp_async8(dst + m, src0 + (long)m * a.se);
+    } else {
+      // a row edge: the valid line alone, the empty one zero
+      T *da = reinterpret_cast<T *>(dst), *db = da + 1;
+      for (int m = threadIdx.x >> (a.lg_lines - 1); m < n; m += ms) {
+        if (offa >= 0) cp_async4(da + 2 * m, a.data + offa + (long)m * a.se); else da[2 * m] = T(0);
+        if (offb >= 0) cp_async4(db + 2 * m, a.data + offb + (long)m * a.se); else db[2 * m] = T(0);
+      }
+    }
+  } else if (a.line_fast) {
     const int l = threadIdx.x & (nl - 1);
     const long off = table.off[l];
     T *dst = reinterpret_cast<T *>(s + (l >> 1) * ROW) + (l & 1);
@@ -669,7 +696,27 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
     if (2 * m <= L) return comp ? (xm.y + xn.y) * h : (xm.x + xn.x) * h;
     return comp ? (xm.x - xn.x) * h : (xn.y - xm.y) * h;
   };
-  if (a.line_fast) {
+  if (a.line_fast && a.pair8) {
+    // one 8-byte store per point for a pair of adjacent lines
+    const int p = threadIdx.x & (a.P - 1), ms = blockDim.x >> (a.lg_lines - 1);
+    const long offa = table.off[2 * p], offb = table.off[2 * p + 1];
+    const T2 *r = s + p * ROW;
+    if (offa >= 0 && offb >= 0) {
+      T2 *dst0 = reinterpret_cast<T2 *>(a.data + offa);
+      const long se2 = a.se / 2;
+      for (int m = threadIdx.x >> (a.lg_lines - 1); m < n; m += ms) {
+        T2 o;
+        o.x = value(r, m, 0);
+        o.y = value(r, m, 1);
+        dst0[(long)m * se2] = o;
+      }
+    } else {
+      for (int m = threadIdx.x >> (a.lg_lines - 1); m < n; m += ms) {
+        if (offa >= 0) a.data[offa + (long)m * a.se] = value(r, m, 0);
+        if (offb >= 0) a.data[offb + (long)m * a.se] = value(r, m, 1);
+      }
+    }
+  } else if (a.line_fast) {
     const int l = threadIdx.x & (nl - 1);
     const long off = table.off[l];
     if (off >= 0) {
@@ -967,6 +1014,9 @@ static LineArgs<T> make_args(const Geometry &g, const AxisPlan<T> &ax, int d, T 
   a.P = ax.P;
   a.lg_lines = ax.lg_lines;
   a.line_fast = ax.line_fast ? 1 : 0;
+  a.na_lines = a.na;
+  a.lead = 0;
+  a.pair8 = 0;
   a.scale = 1.0;
   return a;
 }
@@ -983,7 +1033,15 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
     LineArgs<T> a = make_args(g, ax, d, phi);
     a.scale = scale;
     if (mode == kModeFwdEigInv) a.eig = eig;  // the z sweep's other axes are x (fast) and y
-    const long total = (long)a.na * a.nb;
+    if (ax.reg_n1 && a.line_fast && a.sa == 1 && a.se % 2 == 0 && a.sb % 2 == 0) {
+      // strided lines along x-adjacent columns: enumerate them from an even
+      // address (lead: the odd owner origin of a periodic x axis) in rows of
+      // an even count, so every pair is one aligned 8-byte element
+      a.lead = (int)(a.base % 2);
+      a.na_lines = (a.na + a.lead + 1) / 2 * 2;
+      a.pair8 = 1;
+    }
+    const long total = (long)a.na_lines * a.nb;
     if (ax.reg_n1) {
       a.P = ax.reg_P;
       a.lg_lines = ax.reg_lg;
