@@ -610,16 +610,14 @@ __global__ void periodic_kernel(Geometry g, T *f0, T *f1, T *f2, int scalar, Res
 // Each thread owns KZ consecutive owner planes of one (i, j) column; the
 // loads of all its points are issued before any result is stored.
 constexpr int kDivKZ = 4;
-// The compensated variant reads five more values per point (the residuals):
-// two planes per thread keep it near the plain kernel's register count.
+// The compensated divergence (divergence_pair_kernel) reads five more
+// values per point, the residuals: two planes per thread keep its register
+// count near the plain kernel's.
 constexpr int kDivKZComp = 2;
 
-// kComp: the velocity is hi + residual; each difference adds the residuals'
-// difference, so the float divergence sees the compensated state.
-template <typename T, bool kComp, int KZ = kComp ? kDivKZComp : kDivKZ>
+template <typename T, int KZ = kDivKZ>
 __global__ void __launch_bounds__(128) divergence_kernel(Geometry g, T *__restrict__ phi, const T *__restrict__ u,
-                                                         const T *__restrict__ v, const T *__restrict__ w, T inv_dt,
-                                                         Residual res) {
+                                                         const T *__restrict__ v, const T *__restrict__ w, T inv_dt) {
   const int i = g.own_lo[0] + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = g.own_lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
   const int kb = g.own_lo[2] + blockIdx.z * KZ;
@@ -627,10 +625,7 @@ __global__ void __launch_bounds__(128) divergence_kernel(Geometry g, T *__restri
   if (i >= g.own_lo[0] + g.np[0] || j >= g.own_lo[1] + g.np[1]) return;
   const long q0 = g.idx(i, j, kb), sy = g.sy(), sz = g.sz();
   T a[KZ], b[KZ], c[KZ], d[KZ], e[KZ + 1];
-  float la[KZ], lb[KZ], lc[KZ], ldd[KZ], le[KZ + 1];
-  auto rl = [&](int comp, long q) { return __bfloat162float(__ldg(res.c[comp] + q)); };
   e[0] = ld(w, q0);
-  if constexpr (kComp) le[0] = rl(2, q0);
 #pragma unroll
   for (int r = 0; r < KZ; ++r) {
     if (kb + r >= ke) break;
@@ -640,27 +635,91 @@ __global__ void __launch_bounds__(128) divergence_kernel(Geometry g, T *__restri
     c[r] = ld(v, q + sy);
     d[r] = ld(v, q);
     e[r + 1] = ld(w, q + sz);
-    if constexpr (kComp) {
-      la[r] = rl(0, q + 1);
-      lb[r] = rl(0, q);
-      lc[r] = rl(1, q + sy);
-      ldd[r] = rl(1, q);
-      le[r + 1] = rl(2, q + sz);
-    }
   }
 #pragma unroll
   for (int r = 0; r < KZ; ++r) {
     if (kb + r >= ke) break;
-    T du = a[r] - b[r], dv = c[r] - d[r], dw = e[r + 1] - e[r];
-    if constexpr (kComp) {
-      du += la[r] - lb[r];
-      dv += lc[r] - ldd[r];
-      dw += le[r + 1] - le[r];
-    }
-    du = du * T(g.oh[0]);
-    dv = dv * T(g.oh[1]);
-    dw = dw * T(g.oh[2]);
+    const T du = (a[r] - b[r]) * T(g.oh[0]);
+    const T dv = (c[r] - d[r]) * T(g.oh[1]);
+    const T dw = (e[r + 1] - e[r]) * T(g.oh[2]);
     phi[q0 + r * sz] = (du + dv + dw) * inv_dt;
+  }
+}
+
+// The compensated divergence: the velocity is hi + residual, and each
+// difference adds the residuals' difference, so the float divergence sees
+// the compensated state: ((a - b) + (la - lb)) / h per axis, summed as in
+// divergence_kernel. Two adjacent x points per thread: the velocity in
+// aligned 8-byte float pairs and the residuals in 4-byte bfloat16 pairs (a
+// pair starts at an even x and PX is even). Pairs run over x from 0; a point
+// outside the owner range is read but not written.
+template <int KZ>
+__global__ void __launch_bounds__(128)
+    divergence_pair_kernel(Geometry g, float *__restrict__ phi, const float *__restrict__ u,
+                           const float *__restrict__ v, const float *__restrict__ w, float inv_dt, Residual res) {
+  const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = g.own_lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int kb = g.own_lo[2] + blockIdx.z * KZ;
+  const int ke = min(kb + KZ, g.own_lo[2] + g.np[2]);
+  const int x_lo = g.own_lo[0], x_hi = g.own_lo[0] + g.np[0];
+  const bool ok0 = i0 >= x_lo && i0 < x_hi, ok1 = i0 + 1 >= x_lo && i0 + 1 < x_hi;
+  if ((!ok0 && !ok1) || j >= g.own_lo[1] + g.np[1]) return;
+  const long q0 = g.idx(i0, j, kb), sy = g.sy(), sz = g.sz();
+  auto f2 = [](const float *f, long q) { return __ldg(reinterpret_cast<const float2 *>(f + q)); };
+  auto b2 = [](const __nv_bfloat16 *f, long q) {
+    return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162 *>(f + q)));
+  };
+  float2 ua[KZ], va[KZ], vb[KZ], we[KZ + 1], lua[KZ], lva[KZ], lvb[KZ], lwe[KZ + 1];
+  float u2[KZ], lu2[KZ];
+  we[0] = f2(w, q0);
+  lwe[0] = b2(res.c[2], q0);
+#pragma unroll
+  for (int r = 0; r < KZ; ++r) {
+    if (kb + r >= ke) break;
+    const long q = q0 + r * sz;
+    ua[r] = f2(u, q);
+    va[r] = f2(v, q);
+    vb[r] = f2(v, q + sy);
+    we[r + 1] = f2(w, q + sz);
+    lua[r] = b2(res.c[0], q);
+    lva[r] = b2(res.c[1], q);
+    lvb[r] = b2(res.c[1], q + sy);
+    lwe[r + 1] = b2(res.c[2], q + sz);
+    // u one point past the pair, for its second point
+    u2[r] = ok1 ? __ldg(u + q + 2) : 0.f;
+    lu2[r] = ok1 ? __bfloat162float(__ldg(res.c[0] + q + 2)) : 0.f;
+  }
+  const float oh0 = float(g.oh[0]), oh1 = float(g.oh[1]), oh2 = float(g.oh[2]);
+#pragma unroll
+  for (int r = 0; r < KZ; ++r) {
+    if (kb + r >= ke) break;
+    float du = ua[r].y - ua[r].x, dv = vb[r].x - va[r].x, dw = we[r + 1].x - we[r].x;
+    du += lua[r].y - lua[r].x;
+    dv += lvb[r].x - lva[r].x;
+    dw += lwe[r + 1].x - lwe[r].x;
+    du = du * oh0;
+    dv = dv * oh1;
+    dw = dw * oh2;
+    float2 out;
+    out.x = (du + dv + dw) * inv_dt;
+    du = u2[r] - ua[r].y;
+    dv = vb[r].y - va[r].y;
+    dw = we[r + 1].y - we[r].y;
+    du += lu2[r] - lua[r].y;
+    dv += lvb[r].y - lva[r].y;
+    dw += lwe[r + 1].y - lwe[r].y;
+    du = du * oh0;
+    dv = dv * oh1;
+    dw = dw * oh2;
+    out.y = (du + dv + dw) * inv_dt;
+    const long q = q0 + r * sz;
+    if (ok0 && ok1) {
+      *reinterpret_cast<float2 *>(phi + q) = out;
+    } else if (ok0) {
+      phi[q] = out.x;
+    } else {
+      phi[q + 1] = out.y;
+    }
   }
 }
 
@@ -727,15 +786,14 @@ __global__ void neumann_flux_data_kernel(Geometry g, T *phi, const double *G, Gr
 // projection measured 2.76 / 2.44 / 2.77 / 3.13 ms per step for 1 / 2 / 4 / 8.
 constexpr int kProjKZ = 2;
 
-// kComp: the velocity update is an error-free sum into hi + residual.
 // nonfinite (may be null): set to 1 when a phi value read is NaN or Inf. A
 // NaN or Inf anywhere in the velocity reaches every phi value through the
 // divergence and the spectral solve, so this one check per point watches
 // the whole step.
-template <typename T, bool kComp>
+template <typename T>
 __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict__ p, const T *__restrict__ phi,
                                                       T *__restrict__ u, T *__restrict__ v, T *__restrict__ w, T dt,
-                                                      TimeRef tr, unsigned tag, Residual res, int *nonfinite) {
+                                                      TimeRef tr, unsigned tag, int *nonfinite) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int kb = blockIdx.z * kProjKZ;
@@ -743,7 +801,6 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
   T *vel[3] = {u, v, w};
   const long sc[3] = {1, sy, sz};
   T ph[kProjKZ + 1], nb[2][kProjKZ], pv[kProjKZ], vv[3][kProjKZ];
-  float lv[3][kProjKZ];
   // loads: phi at the points, their -x and -y neighbours, the plane below, p and the velocity
   ph[0] = (kb >= 1 && i < g.E[0] && j < g.E[1] && kb - 1 < g.E[2]) ? ld(phi, g.idx(i, j, kb - 1)) : T(0);
 #pragma unroll
@@ -759,7 +816,6 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
     for (int c = 0; c < 3; ++c) {
       const bool in = i >= 1 && j >= 1 && k >= 1 && i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
       vv[c][r] = in ? vel[c][q] : T(0);
-      if constexpr (kComp) lv[c][r] = in ? __bfloat162float(res.c[c][q]) : 0.f;
     }
   }
   constexpr bool kSR = std::is_same<T, float>::value;
@@ -783,13 +839,108 @@ __global__ void __launch_bounds__(128) project_kernel(Geometry g, T *__restrict_
       if (i < 1 || j < 1 || k < 1 || i >= g.ext(c, 0) - 1 || j >= g.ext(c, 1) - 1 || k >= g.ext(c, 2) - 1) continue;
       const T below = c == 0 ? nb[0][r] : (c == 1 ? nb[1][r] : ph[r]);
       const T gp = (ph[r + 1] - below) * T(g.oh[c]);
-      if constexpr (kComp)
-        vel[c][q] = comp_add(vv[c][r], lv[c][r], -(gp * dt), res.c[c] + q);
-      else
-        vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_draw(h, c)) : vv[c][r] - gp * dt;
+      vel[c][q] = kSR ? state_add(vv[c][r], -(gp * dt), sr_draw(h, c)) : vv[c][r] - gp * dt;
     }
   }
   (void)sc;
+}
+
+// The compensated projection: the masks, the gradient and the pressure's
+// stochastically rounded update of project_kernel, with the velocity update
+// an error-free sum into hi + residual (comp_add). Two adjacent x points and
+// one plane per thread: phi, p, the velocity and the residuals in aligned
+// pairs (8-byte floats, 4-byte bfloat16 pairs). A pair whose two points need
+// different updates stores them one by one.
+__global__ void __launch_bounds__(128)
+    project_pair_kernel(Geometry g, float *__restrict__ p, const float *__restrict__ phi, float *__restrict__ u,
+                        float *__restrict__ v, float *__restrict__ w, float dt, TimeRef tr, unsigned tag,
+                        Residual res, int *nonfinite) {
+  const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i0 >= g.PX || j >= g.PY) return;
+  const long sy = g.sy(), sz = g.sz();
+  const long q = g.idx(i0, j, k);
+  float *vel[3] = {u, v, w};
+  auto f2 = [](const float *f, long qq) { return *reinterpret_cast<const float2 *>(f + qq); };
+  const bool jk_in = j < g.E[1] && k < g.E[2];
+  const bool inp[2] = {jk_in && i0 < g.E[0], jk_in && i0 + 1 < g.E[0]};
+  float2 ph = make_float2(0.f, 0.f), below_z = make_float2(0.f, 0.f), below_y = make_float2(0.f, 0.f);
+  float below_x0 = 0.f, pv[2] = {0.f, 0.f};
+  if (inp[0] || inp[1]) {
+    const float2 a = __ldg(reinterpret_cast<const float2 *>(phi + q));
+    ph = make_float2(inp[0] ? a.x : 0.f, inp[1] ? a.y : 0.f);
+    if (k >= 1) {
+      const float2 b = __ldg(reinterpret_cast<const float2 *>(phi + q - sz));
+      below_z = make_float2(inp[0] ? b.x : 0.f, inp[1] ? b.y : 0.f);
+    }
+    if (j >= 1) {
+      const float2 b = __ldg(reinterpret_cast<const float2 *>(phi + q - sy));
+      below_y = make_float2(inp[0] ? b.x : 0.f, inp[1] ? b.y : 0.f);
+    }
+    if (inp[0] && i0 >= 1) below_x0 = __ldg(phi + q - 1);
+    const float2 pp = f2(p, q);
+    pv[0] = pp.x;
+    pv[1] = pp.y;
+  }
+  // interior of component c at the two points, their values and residuals
+  bool in[3][2];
+  float2 vv[3], lv[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const bool jk = j >= 1 && k >= 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
+    in[c][0] = jk && i0 >= 1 && i0 < g.ext(c, 0) - 1;
+    in[c][1] = jk && i0 + 1 < g.ext(c, 0) - 1;
+    vv[c] = make_float2(0.f, 0.f);
+    lv[c] = make_float2(0.f, 0.f);
+    if (in[c][0] || in[c][1]) {
+      vv[c] = f2(vel[c], q);
+      lv[c] = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(res.c[c] + q));
+    }
+  }
+  if (nonfinite && !(isfinite(ph.x) && isfinite(ph.y) && isfinite(below_z.x) && isfinite(below_z.y)))
+    *nonfinite = 1;
+  const unsigned salt = sr_salt(tr, tag);
+  float pout[2];
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float phe = e ? ph.y : ph.x;
+    const unsigned h = sr_mix((unsigned)(q + e) ^ salt);
+    pout[e] = state_add(pv[e], phe, sr_draw(sr_mix(h), 0));
+  }
+  if (inp[0] && inp[1])
+    *reinterpret_cast<float2 *>(p + q) = make_float2(pout[0], pout[1]);
+  else if (inp[0])
+    p[q] = pout[0];
+  else if (inp[1])
+    p[q + 1] = pout[1];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (!in[c][0] && !in[c][1]) continue;
+    float out[2];
+    __nv_bfloat16 lo[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const float phe = e ? ph.y : ph.x;
+      const float below = c == 0 ? (e ? ph.x : below_x0) : (c == 1 ? (e ? below_y.y : below_y.x)
+                                                                    : (e ? below_z.y : below_z.x));
+      const float gp = (phe - below) * float(g.oh[c]);
+      out[e] = comp_add(e ? vv[c].y : vv[c].x, e ? lv[c].y : lv[c].x, -(gp * dt), lo + e);
+    }
+    if (in[c][0] && in[c][1]) {
+      *reinterpret_cast<float2 *>(vel[c] + q) = make_float2(out[0], out[1]);
+      __nv_bfloat162 l2;
+      l2.x = lo[0];
+      l2.y = lo[1];
+      *reinterpret_cast<__nv_bfloat162 *>(res.c[c] + q) = l2;
+    } else if (in[c][0]) {
+      vel[c][q] = out[0];
+      res.c[c][q] = lo[0];
+    } else {
+      vel[c][q + 1] = out[1];
+      res.c[c][q + 1] = lo[1];
+    }
+  }
 }
 
 // ---- layout conversion and initial fields ----
@@ -1166,14 +1317,18 @@ template <typename T>
 void launch_divergence(const Geometry &g, T *phi, T *const vel[3], double dt, cudaStream_t s, long long *launches,
                        const Residual &res) {
   const dim3 blk(32, 4, 1);
-  if (std::is_same<T, float>::value && res.on()) {
-    const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZComp));
-    divergence_kernel<T, std::is_same<T, float>::value><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2],
-                                                                             T(1.0 / dt), res);
-  } else {
-    const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZ));
-    divergence_kernel<T, false><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt), res);
+  if constexpr (std::is_same<T, float>::value) {
+    if (res.on()) {
+      // x pairs from x = 0 up to the owner range's end
+      const int pairs = (g.own_lo[0] + g.np[0] + 1) / 2;
+      const dim3 grid(cdiv(pairs, 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZComp));
+      divergence_pair_kernel<kDivKZComp><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt), res);
+      if (launches) ++*launches;
+      return;
+    }
   }
+  const dim3 grid(cdiv(g.np[0], 32), cdiv(g.np[1], 4), cdiv(g.np[2], kDivKZ));
+  divergence_kernel<T><<<grid, blk, 0, s>>>(g, phi, vel[0], vel[1], vel[2], T(1.0 / dt));
   if (launches) ++*launches;
 }
 
@@ -1201,12 +1356,15 @@ void launch_project(const Geometry &g, T *p, const T *phi, T *const vel[3], doub
   const dim3 blk(32, 4, 1);
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
   const dim3 grid(cdiv(ni, 32), cdiv(g.Es[1], 4), cdiv(g.Es[2], kProjKZ));
-  if (std::is_same<T, float>::value && res.on())
-    project_kernel<T, std::is_same<T, float>::value><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt),
-                                                                          tr, tag, res, nonfinite);
-  else
-    project_kernel<T, false><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt), tr, tag, res,
-                                                  nonfinite);
+  if constexpr (std::is_same<T, float>::value) {
+    if (res.on()) {
+      const dim3 pgrid(cdiv((ni + 1) / 2, 32), cdiv(g.Es[1], 4), (unsigned)g.Es[2]);
+      project_pair_kernel<<<pgrid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt), tr, tag, res, nonfinite);
+      if (launches) ++*launches;
+      return;
+    }
+  }
+  project_kernel<T><<<grid, blk, 0, s>>>(g, p, phi, vel[0], vel[1], vel[2], T(dt), tr, tag, nonfinite);
   if (launches) ++*launches;
 }
 
