@@ -304,8 +304,12 @@ __device__ __forceinline__ T rhs_taps(int c, const Taps<T> &a, const Coeffs<T> &
 // kComp (float only, projection stages): the input state is hi + residual
 // and the output state is written as an error-free sum (comp_add) into its
 // float field and the residual, in place (Residual).
+// Resident CTAs per SM the register budget is sized for: float, the
+// compensated float variant, double.
+constexpr int kStageMinBlocksF32 = 12, kStageMinBlocksComp = 12, kStageMinBlocksF64 = 4;
 template <typename T, int ST, bool kComp>
-__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? 12 : 4)
+__global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinBlocksComp : kStageMinBlocksF32)
+                                                           : kStageMinBlocksF64)
     stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K, int forcing, ForcingEval<T> fe,
                        TimeRef tr, int sin_slot, int kc, Residual res) {
   constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
@@ -528,44 +532,49 @@ __device__ TE face_value(const Geometry &g, int c, int d, int s, const long *pt,
   return s == 0 ? base + TE(g.h_2[d]) * sum : base - TE(g.h_2[d]) * sum;
 }
 
-// blockIdx.z = c * 3 + d: component c, faces normal to axis d. Each face
-// point is written once, by the face the reference writes last (order
-// z_min, z_max, y_min, y_max, x_min, x_max).
+// blockIdx.z = d: faces normal to axis d; one thread takes face point
+// (pa, pb) of all three components, both sides. Each face point is written
+// once, by the face the reference writes last (order z_min, z_max, y_min,
+// y_max, x_min, x_max).
 template <typename T>
 __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int fn, TimeRef tr, int t_slot,
                                 FaceTables ft, Residual res) {
-  const int c = blockIdx.z / 3, d = blockIdx.z % 3;
-  const double t = tr.get(t_slot);
-  // caller data (slot_stride > 0): the slot's own table, no time factor
-  const double factor = ft.tab ? (ft.slot_stride ? 1.0 : tr.get(kSlotFactor + 4 * fn + t_slot)) : 0.0;
-  const double *tab = ft.tab ? ft.tab + (long)t_slot * ft.slot_stride : nullptr;
+  const int d = blockIdx.z;
   if (g.periodic[d]) return;
   const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
   const long pa = blockIdx.x * blockDim.x + threadIdx.x;
   const long pb = blockIdx.y * blockDim.y + threadIdx.y;
-  if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) return;
-  T *f = c == 0 ? c0 : (c == 1 ? c1 : c2);
-  for (int s = 0; s < 2; ++s) {
-    long pt[3];
-    pt[a] = pa;
-    pt[b] = pb;
-    pt[d] = s == 0 ? 0 : g.ext(c, d) - 1;
-    bool later = false;  // an x face beats y beats z
-    for (int d2 = 0; d2 < d; ++d2)
-      if (!g.periodic[d2] && (pt[d2] == 0 || pt[d2] == g.ext(c, d2) - 1)) later = true;
-    if (later) continue;
-    const long q = g.idx(pt[0], pt[1], pt[2]);
-    if constexpr (std::is_same<T, float>::value) {
-      if (res.on()) {  // compensated state: the double face value as hi + residual
-        const double v = tab ? tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor
-                             : (double)face_value<T>(g, c, d, s, pt, kind, fn, T(t));
-        f[q] = comp_split(v, res.c[c] + q);
-        continue;
+  if (pa >= g.Es[a] || pb >= g.Es[b]) return;  // the widest extents of the three components
+  const double t = tr.get(t_slot);
+  // caller data (slot_stride > 0): the slot's own table, no time factor
+  const double factor = ft.tab ? (ft.slot_stride ? 1.0 : tr.get(kSlotFactor + 4 * fn + t_slot)) : 0.0;
+  const double *tab = ft.tab ? ft.tab + (long)t_slot * ft.slot_stride : nullptr;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) continue;
+    T *f = c == 0 ? c0 : (c == 1 ? c1 : c2);
+    for (int s = 0; s < 2; ++s) {
+      long pt[3];
+      pt[a] = pa;
+      pt[b] = pb;
+      pt[d] = s == 0 ? 0 : g.ext(c, d) - 1;
+      bool later = false;  // an x face beats y beats z
+      for (int d2 = 0; d2 < d; ++d2)
+        if (!g.periodic[d2] && (pt[d2] == 0 || pt[d2] == g.ext(c, d2) - 1)) later = true;
+      if (later) continue;
+      const long q = g.idx(pt[0], pt[1], pt[2]);
+      if constexpr (std::is_same<T, float>::value) {
+        if (res.on()) {  // compensated state: the double face value as hi + residual
+          const double v = tab ? tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor
+                               : (double)face_value<T>(g, c, d, s, pt, kind, fn, T(t));
+          f[q] = comp_split(v, res.c[c] + q);
+          continue;
+        }
       }
+      const T val = tab ? T(tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor)
+                        : T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
+      f[q] = val;
     }
-    const T val = tab ? T(tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor)
-                      : T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
-    f[q] = val;
   }
 }
 
@@ -1250,7 +1259,7 @@ void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn
   int mx = 0;
   for (int d = 0; d < 3; ++d) mx = mx > g.Es[d] ? mx : g.Es[d];
   if (!(g.periodic[0] && g.periodic[1] && g.periodic[2])) {
-    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 9);
+    const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 3);
     bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft, res);
     if (launches) ++*launches;
   }
