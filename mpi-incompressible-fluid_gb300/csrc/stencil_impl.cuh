@@ -535,8 +535,10 @@ __device__ TE face_value(const Geometry &g, int c, int d, int s, const long *pt,
 // blockIdx.z = d: faces normal to axis d; one thread takes face point
 // (pa, pb) of all three components, both sides. Each face point is written
 // once, by the face the reference writes last (order z_min, z_max, y_min,
-// y_max, x_min, x_max).
-template <typename T>
+// y_max, x_min, x_max). kTable: the values come from the double face tables
+// only (ft.tab set), so the analytic families' code, and the registers it
+// needs, are left out of that instantiation.
+template <typename T, bool kTable>
 __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int fn, TimeRef tr, int t_slot,
                                 FaceTables ft, Residual res) {
   const int d = blockIdx.z;
@@ -554,25 +556,31 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
     if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) continue;
     T *f = c == 0 ? c0 : (c == 1 ? c1 : c2);
     for (int s = 0; s < 2; ++s) {
-      long pt[3];
-      pt[a] = pa;
-      pt[b] = pb;
-      pt[d] = s == 0 ? 0 : g.ext(c, d) - 1;
+      // the point's (x, y, z): the face's fixed coordinate along d, pa and pb
+      // along the other two axes in order
+      const long fixed = s == 0 ? 0 : g.ext(c, d) - 1;
+      const long pt[3] = {d == 0 ? fixed : pa, d == 1 ? fixed : (d == 0 ? pa : pb), d == 2 ? fixed : pb};
       bool later = false;  // an x face beats y beats z
-      for (int d2 = 0; d2 < d; ++d2)
-        if (!g.periodic[d2] && (pt[d2] == 0 || pt[d2] == g.ext(c, d2) - 1)) later = true;
+      if (d >= 1 && !g.periodic[0] && (pt[0] == 0 || pt[0] == g.ext(c, 0) - 1)) later = true;
+      if (d == 2 && !g.periodic[1] && (pt[1] == 0 || pt[1] == g.ext(c, 1) - 1)) later = true;
       if (later) continue;
       const long q = g.idx(pt[0], pt[1], pt[2]);
       if constexpr (std::is_same<T, float>::value) {
         if (res.on()) {  // compensated state: the double face value as hi + residual
-          const double v = tab ? tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor
-                               : (double)face_value<T>(g, c, d, s, pt, kind, fn, T(t));
+          double v;
+          if constexpr (kTable)
+            v = tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor;
+          else
+            v = (double)face_value<T>(g, c, d, s, pt, kind, fn, T(t));
           f[q] = comp_split(v, res.c[c] + q);
           continue;
         }
       }
-      const T val = tab ? T(tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor)
-                        : T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
+      T val;
+      if constexpr (kTable)
+        val = T(tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor);
+      else
+        val = T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
       f[q] = val;
     }
   }
@@ -1260,7 +1268,11 @@ void launch_apply_bc(const Geometry &g, T *const comp[3], int field_kind, int fn
   for (int d = 0; d < 3; ++d) mx = mx > g.Es[d] ? mx : g.Es[d];
   if (!(g.periodic[0] && g.periodic[1] && g.periodic[2])) {
     const dim3 grid(cdiv(mx, 32), cdiv(mx, 8), 3);
-    bc_faces_kernel<T><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft, res);
+    if (ft.tab)
+      bc_faces_kernel<T, true><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft, res);
+    else
+      bc_faces_kernel<T, false><<<grid, blk, 0, s>>>(g, comp[0], comp[1], comp[2], field_kind, fn, tr, t_slot, ft,
+                                                     res);
     if (launches) ++*launches;
   }
   if (g.periodic[0] || g.periodic[1] || g.periodic[2]) {

@@ -1,8 +1,9 @@
 """The benchmark's full size (the 512^3 Ethier-Steinman cube, 513^3 nodes),
 checked through properties that do not need the oracle at that size: two
-steps in FP64 and in mixed precision each stay within their known distance
-of the exact solution (FP64 8.0e-7 and mixed 1.3e-6 in L-infinity at this
-dt), and the mixed fields stay within float rounding of the FP64 ones. The
+steps in FP64, in the plain float mode and in the compensated float state
+each stay within their known distance of the exact solution (FP64 8.0e-7 and
+mixed 1.3e-6 in L-infinity at this dt; the compensated state within 1 % of
+FP64's), and the float fields stay within rounding of the FP64 ones. The
 FP64 path itself is pinned to the oracle on the smaller grids."""
 import numpy as np
 import pytest
@@ -28,6 +29,13 @@ def run(mg, precision):
 def test_full_size_steps_fp64_and_mixed(mifgpu_lib, cuda_device):
     n64, f64 = run(mifgpu_lib, mifgpu_lib.FP64)
     nmx, fmx = run(mifgpu_lib, mifgpu_lib.MIXED)
+    ncp, fcp = run(mifgpu_lib, mifgpu_lib.MIXED_COMPENSATED)
+    # the compensated state: the FP64 error within 1 %, and the fields within
+    # 2e-7 of FP64's (the plain float mode's bound below is 1e-5)
+    assert ncp[2] <= 1.01 * n64[2], (ncp[2], n64[2])
+    for n in ("u", "w"):
+        scale = np.abs(f64[n]).max()
+        assert np.abs(fcp[n] - f64[n]).max() <= 2e-7 * scale, n
     # velocity L-infinity against the exact solution (norms[2])
     assert n64[2] < 1.0e-6, n64[2]
     assert nmx[2] < 3.0e-6, nmx[2]
