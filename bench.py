@@ -100,17 +100,33 @@ LAUNCHES_PER_STEP = {"stage": 3, "divergence": 3, "x_forward": 3, "y_forward": 3
 
 
 def sweeps(precision: str) -> dict:
+    """Per launch (the stage class: the mean of the step's three stages)."""
     out = dict(SWEEPS)
     if precision == "compensated":
         for k, v in COMPENSATED_EXTRA.items():
             out[k] += v
+        # The Y3 and U* stage kernels apply the projection before them
+        # (stage_proj_kernel): each also reads phi and writes p + phi.
+        out["stage"] += 4.0 / 3.0
+    return out
+
+
+def launches_per_step(precision: str) -> dict:
+    """In the compensated state only the step's last projection is a kernel of its own."""
+    out = dict(LAUNCHES_PER_STEP)
+    if precision == "compensated":
+        out["project"] = 1
     return out
 
 
 def step_sweeps(precision: str) -> float:
     """Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps +
-    9 projection) = 102; the compensated state adds 3 x (3 + 1.5 + 3) = 22.5."""
-    return sum(v * LAUNCHES_PER_STEP[k] for k, v in sweeps(precision).items())
+    9 projection) = 102 in FP64 and the plain float mode. The compensated
+    state: stages 13 + 18 + 15 (residuals, and phi and p + phi in the two
+    stages that project), 3 x 5.5 divergence, 30 line sweeps and one
+    projection of 12: 104.5."""
+    n = launches_per_step(precision)
+    return sum(v * n[k] for k, v in sweeps(precision).items())
 
 
 # DRAM read + write bytes over algorithmic bytes, from ncu captures of the
@@ -852,10 +868,11 @@ def run_gpu(args):
     t += 2 * dt
     peak, peak_kind = measured_peaks()
     sw = sweeps(prec)
+    nl = launches_per_step(prec)
     classes = {k: v for k, v in prof.items() if k in sw}
     dom = max(classes, key=lambda k: classes[k])
     alg_bytes_launch = sw[dom] * elem * cells
-    avg_launch_ms = classes[dom] / LAUNCHES_PER_STEP[dom]
+    avg_launch_ms = classes[dom] / nl[dom]
     achieved = alg_bytes_launch / (avg_launch_ms / 1e3) / 1e9
     # DRAM traffic per launch from one ncu capture of the same kernels on a
     # profiling case: measured read+write bytes over algorithmic bytes,
@@ -869,8 +886,8 @@ def run_gpu(args):
     ssw = step_sweeps(prec)
     step_roofline = ssw * elem * cells / (step_ms / 1e3) / 1e9
     per_kernel = {k: {"ms_per_step": round(v, 4),
-                      "gbs": round(sw[k] * LAUNCHES_PER_STEP[k] * elem * cells / (v / 1e3) / 1e9, 1),
-                      "frac": round(sw[k] * LAUNCHES_PER_STEP[k] * elem * cells / (v / 1e3) / 1e9 / peak, 4)}
+                      "gbs": round(sw[k] * nl[k] * elem * cells / (v / 1e3) / 1e9, 1),
+                      "frac": round(sw[k] * nl[k] * elem * cells / (v / 1e3) / 1e9 / peak, 4)}
                   for k, v in classes.items() if v > 0}
 
     # end to end through the drop-in host call, pinned host buffers

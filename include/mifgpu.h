@@ -56,7 +56,11 @@ enum mifgpu_precision {
                        transforms still read float. Host transfers of velocity
                        set 0 and the error norms see hi + residual. The
                        velocity-only step and the reverse mode return
-                       MIFGPU_ENOTSUP in this mode. */
+                       MIFGPU_ENOTSUP in this mode. Inside a step the Y3 and U*
+                       stage kernels apply the projection before them, so after
+                       a step velocity_buffer and velocity_buffer_2 (scratch in
+                       the reference too) hold the unprojected stage states;
+                       the context holds one more pressure-sized buffer. */
 };
 
 /* Analytic field families used for Dirichlet boundary data, forcing and

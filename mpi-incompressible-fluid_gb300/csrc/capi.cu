@@ -201,6 +201,10 @@ struct Impl final : ImplBase {
   // (one triple shared by the three sets, see Residual).
   __nv_bfloat16 *res_block = nullptr;
   Residual res{};
+  // ... and the second pressure buffer of the stages that apply the preceding
+  // projection themselves (StageProj: the Y3 stage writes p + phi here, the
+  // U* stage reads it and writes the pressure field).
+  T *p_alt = nullptr;
   double *face_tab = nullptr;  // float path: the families' face data in double; or the caller's
   FaceTables ftabs{};
   // Caller pressure-gradient face data (slots 0..3), allocated on first use.
@@ -253,6 +257,7 @@ struct Impl final : ImplBase {
     cudaFree(staging);
     cudaFree(grad_block);
     cudaFree(res_block);
+    cudaFree(p_alt);
     cudaFree(face_tab);
     cudaFree(grad_tab);
     cudaFree(adj_block);
@@ -290,6 +295,10 @@ struct Impl final : ImplBase {
       total_bytes += sizeof(__nv_bfloat16) * field_elems * 3;
       CK(cudaMemset(res_block, 0, sizeof(__nv_bfloat16) * field_elems * 3));
       for (int c = 0; c < 3; ++c) res.c[c] = res_block + c * field_elems;
+      if (cudaMalloc(&p_alt, sizeof(T) * field_elems) != cudaSuccess)
+        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the second pressure buffer failed");
+      total_bytes += sizeof(T) * field_elems;
+      CK(cudaMemset(p_alt, 0, sizeof(T) * field_elems));
     }
     std::string perr;
     const int rc = ps.init(g, perr);
@@ -638,15 +647,28 @@ struct Impl final : ImplBase {
     const StageKind kinds[3] = {kStageY2, kStageY3, kStageUStar};
     const int out_set[3] = {1, 2, 0};
     const int sin_slot[3] = {4, 6, 8};
+    // In the compensated state the Y3 and U* stage kernels apply the
+    // projection before them (StageProj): the projected sets 1 and 2 are read
+    // by those stages only, so they are never stored. The pressure goes
+    // p -> p_alt (Y3) -> p (U*), and the last projection is a kernel of its own.
+    const bool fused = res.on() && p_alt;
     for (int st = 0; st < 3; ++st) {
       StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing, ctx->prm.forcing_amplitude};
+      StageProj pj{};
+      if constexpr (std::is_same<T, float>::value) {
+        pj.phi = F.f[kPhi];
+        pj.p_in = st == 1 ? F.f[kP] : p_alt;
+        pj.p_out = st == 1 ? p_alt : F.f[kP];
+        pj.dt = float(dts[st - 1 < 0 ? 0 : st - 1]);
+        pj.tag = 16u + (st - 1 < 0 ? 0 : st - 1);
+      }
       // in the compensated state every stage's output set carries the residuals
       mark(MIFGPU_PROF_STAGE, s);
-      launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res);
+      launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res, fused && st > 0 ? &pj : nullptr);
       enqueue_bc(ctx, s, out_set[st], 1 + st, cnt, res);
       enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt, res);
       // the last projection of the step watches phi for NaN / Inf
-      enqueue_project(s, out_set[st], dts[st], 16u + st, cnt, res, st == 2 ? nonfinite : nullptr);
+      if (!fused || st == 2) enqueue_project(s, out_set[st], dts[st], 16u + st, cnt, res, st == 2 ? nonfinite : nullptr);
     }
   }
 

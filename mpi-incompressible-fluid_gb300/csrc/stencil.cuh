@@ -80,11 +80,25 @@ struct StageScalars {
   double alpha;  // amplitude of the Taylor-Green body force
 };
 
+// The projection that precedes a compensated Y3 or U* stage, applied by the
+// stage kernel itself (see stage_proj_kernel): phi of the previous solve, the
+// pressure read (p_in) and written as p + phi (p_out, another buffer), and the
+// previous projection's dt and stochastic-rounding tag (launch_project's).
+struct StageProj {
+  const float *phi = nullptr;
+  const float *p_in = nullptr;
+  float *p_out = nullptr;
+  float dt = 0.f;
+  unsigned tag = 0;
+};
+
 // `res`: the compensated state's residuals (projection stages, float only).
+// `proj` (compensated kStageY3 / kStageUStar only, or null): the preceding
+// projection, done inside the stage.
 template <typename T>
 void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches,
-                  const Residual &res = Residual{});
+                  const Residual &res = Residual{}, const StageProj *proj = nullptr);
 
 // Dirichlet faces (fn 0 velocity family, 1 pressure-gradient family) then the
 // periodic copies, on velocity set `set` (src/VelocityTensor.cpp:36-233).

@@ -489,6 +489,302 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
   (void)sz;
 }
 
+// ---- compensated Y3 / U* stage with the previous projection inside ----
+//
+// In the compensated state the projections that follow the Y2 and Y3 stages
+// (src/Timestep.cpp:97-141) are applied by the next stage kernel to its own
+// plane ring, as each plane arrives. The projected set is read by that next
+// stage only, so the projected velocity never goes back to memory: per step
+// this saves two projection passes (the velocity and residual read and
+// written, twelve float sweeps each) for one more ring field (phi) and the
+// pressure update, written here.
+//
+// Ring values: u' = fl(u + inc), inc = -(((phi - phi_b) * oh) * dt) with
+// phi_b the neighbour one step back along the component's axis, on the
+// points project_pair_kernel updates (interior of the component), the others
+// as they are. The stencils read these float values as they read the
+// projected float field. The state update needs the exact projected state at
+// the thread's own point: projecting a plane, the thread splits its own
+// point's u + inc into u' + e (TwoSum) and keeps lo' = lo + e beside u' (lo
+// the stored residual), so the update adds its increment to u' + lo' with
+// comp_add as the unfused stage does.
+//
+// The pressure p + phi is written stochastically rounded as project_pair_kernel
+// writes it (same draws), into p_out: other CTAs still read p_in as halo. The
+// pressure gradient of the stage uses (p + phi) unrounded, as the difference of
+// p plus the difference of phi. Pressure nodes outside the threads' range
+// (x = 0, y = 0, z = 0 and the last x node of a periodic axis when it falls on
+// the tile halo) are written by the CTAs at those edges.
+
+// phi tile: rows j0 - 2 .. j0 + kTY (kTY + 3), columns x = i0 - 1 .. i0 + 34 at
+// the velocity tiles' pitch, then the column x = i0 - 2 (one value per row).
+constexpr int kPhiRows = kTY + 3, kPhiCol = kHX * kPhiRows, kPhiPL = kPhiCol + 8;
+struct RingProj {
+  float f[4][4][kPL];  // u, v, w, p: slot (k & 3), as Ring
+  float phi[4][kPhiPL];
+};
+// The ring points (hx, hy) outside the CTA's own kTX x kTY: rows hy = 0 and
+// kTY + 1 (hx = 1 .. kTX), then columns hx = 0 and kTX + 1 (hy = 0 .. kTY + 1).
+constexpr int kHaloPts = 2 * kTX + 2 * (kTY + 2);
+// Resident CTAs per SM the register budget is sized for. The kernel is
+// issue-bound (about 750 instructions per point): on GB300 at 512^3 its time
+// was the same at 12, 10 and 8 CTAs per SM with the same spills, and 8 CTAs
+// (64 registers) remove the spills (40 registers: ~100 bytes a thread, 22
+// local loads per warp and point), which took the two stages from 2.67 to
+// 2.48 ms each.
+#ifndef MIFGPU_STAGE_PROJ_BLOCKS
+#define MIFGPU_STAGE_PROJ_BLOCKS 8
+#endif
+constexpr int kStageProjMinBlocks = MIFGPU_STAGE_PROJ_BLOCKS;
+
+template <int ST, bool kForce>
+__global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
+    stage_proj_kernel(Geometry g, Coeffs<float> co, Fields<float> F, StageCoef<float> K, ForcingEval<float> fe,
+                      TimeRef tr, int sin_slot, int kc, Residual res, StageProj pj) {
+  static_assert(ST == kStageY3 || ST == kStageUStar, "the stages that follow a projection");
+  constexpr int in_set = ST == kStageY3 ? 1 : 2, oth_set = ST == kStageY3 ? 2 : 0;
+  __shared__ __align__(16) RingProj ring;
+  if (kForce) {
+    fe.st = float(tr.get(sin_slot));
+    fe.ct = float(tr.get(sin_slot + 1));
+  }
+  // Parameters the plane loop uses, as locals (the lambdas below capture
+  // locals only).
+  const long plane = g.sz(), PX = g.PX;
+  const int PZ = (int)g.PZ;
+  const int lim0 = g.ext(0, 2) - 1, lim1 = g.ext(1, 2) - 1, lim2 = g.ext(2, 2) - 1;
+  const float pdt = pj.dt, oh0 = co.oh[0], oh1 = co.oh[1], oh2 = co.oh[2];
+  const float *const phi_g = pj.phi;
+  float *const p_out = pj.p_out;
+  const int tid = threadIdx.x, tx = tid % kTX, ty = tid / kTX;
+  const int i0 = 1 + blockIdx.x * kTX, j0 = 1 + blockIdx.y * kTY;
+  const int zmax = g.Es[2] - 1;  // interior k < zmax
+  const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
+  // Plane loads (16-byte vectors): threads t and 64 + t (t < 54) copy vector
+  // t of the u, w tiles and of the v, p tiles; threads t < 63 vector t of the
+  // phi tile; the last kPhiRows threads the phi column x = i0 - 2 (4 bytes).
+  // Shared offsets relative to the slot, source offsets within the plane (-1:
+  // a zero vector).
+  constexpr int kVecRow = kHX / 4, kVecPlane = kVecRow * kHY, kVecPhi = kVecRow * kPhiRows;
+  const int vt = tid & 63, half = tid >> 6;
+  int va = -1, va_off = -1, vp = -1, vp_off = -1;
+  if (vt < kVecPlane) {
+    const int hy = vt / kVecRow, hx = (vt - hy * kVecRow) * 4, ii = i0 - 1 + hx, jj = j0 - 1 + hy;
+    va = hy * kHX + hx;
+    va_off = (ii < PX && jj < g.PY) ? ii + (int)PX * jj : -1;
+  }
+  if (tid < kVecPhi) {
+    const int row = tid / kVecRow, hx = (tid - row * kVecRow) * 4, ii = i0 - 1 + hx, jj = j0 - 2 + row;
+    vp = row * kHX + hx;
+    vp_off = (jj >= 0 && ii < PX && jj < g.PY) ? ii + (int)PX * jj : -1;
+  } else if (tid >= kTX * kTY - kPhiRows) {
+    const int row = tid - (kTX * kTY - kPhiRows), ii = i0 - 2, jj = j0 - 2 + row;
+    vp = kPhiCol + row;
+    vp_off = (ii >= 0 && jj >= 0 && jj < g.PY) ? ii + (int)PX * jj : -1;
+  }
+  const float *const src_a = F.f[in_set * kFieldsPerSet + half];
+  const float *const src_b = half ? pj.p_in : F.f[in_set * kFieldsPerSet + 2];
+  auto load_plane = [&](int kk, bool phi_only) {
+    if (kk >= 0 && kk < PZ) {
+      const long po = (long)kk * plane;
+      const int sl = kk & 3;
+      if (!phi_only && va >= 0) {
+        float *d0 = &ring.f[half][sl][va], *d1 = &ring.f[2 + half][sl][va];
+        if (va_off >= 0) {
+          cp_async16_st(d0, src_a + po + va_off);
+          cp_async16_st(d1, src_b + po + va_off);
+        } else {
+          *reinterpret_cast<float4 *>(d0) = make_float4(0.f, 0.f, 0.f, 0.f);
+          *reinterpret_cast<float4 *>(d1) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+      if (vp >= 0) {
+        float *d = &ring.phi[sl][vp];
+        if (vp < kPhiCol) {
+          if (vp_off >= 0)
+            cp_async16_st(d, phi_g + po + vp_off);
+          else
+            *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+          if (vp_off >= 0)
+            cp_async4_st(d, phi_g + po + vp_off);
+          else
+            *d = 0.f;
+        }
+      }
+    }
+    cp_commit();
+  };
+  const int i = i0 + tx, j = j0 + ty;
+  typename ForcingEval<float>::Axis fx{}, fy{}, fz{};
+  if (kForce) {
+    fx = fe.axis(0, min(i, fe.maxE - 1));
+    fy = fe.axis(1, min(j, fe.maxE - 1));
+  }
+  // The other set's value at the point (set 2 for Y3, set 0 for U*) and the
+  // input state's stored residual, prefetched one plane ahead.
+  const bool in_box = i < PX && j < g.PY;
+  const long qij = (long)i + PX * (long)j;
+  const float *const oth0 = F.vel(oth_set, 0) + qij, *const oth1 = F.vel(oth_set, 1) + qij,
+                     *const oth2 = F.vel(oth_set, 2) + qij;
+  const __nv_bfloat16 *const res0 = res.c[0] + qij, *const res1 = res.c[1] + qij, *const res2 = res.c[2] + qij;
+  float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+  __nv_bfloat16 l0 = __float2bfloat16_rn(0.f), l1 = l0, l2 = l0;
+  auto prefetch = [&](int kk) {
+    if (!in_box || kk >= kend) return;
+    const long po = (long)kk * plane;
+    n0 = oth0[po];
+    n1 = oth1[po];
+    n2 = oth2[po];
+    l0 = res0[po];
+    l1 = res1[po];
+    l2 = res2[po];
+  };
+  // Interior masks in x and y of the own point (bits 0-2: component) and of
+  // this thread's halo point (bits 3-5; threads < kHaloPts), whose ring index
+  // is h_r (the phi index is h_r + kHX, one row down in the phi tile).
+  int h_r = 0, h_px = 0;  // h_px: phi index one point back in x (the phi column for hx = 0)
+  unsigned msk = 0;
+  {
+    int hx = 0, hy = 0;
+    if (tid < kTX) hx = tid + 1, hy = 0;
+    else if (tid < 2 * kTX) hx = tid - kTX + 1, hy = kTY + 1;
+    else if (tid < 2 * kTX + kTY + 2) hx = 0, hy = tid - 2 * kTX;
+    else hx = kTX + 1, hy = tid - 2 * kTX - (kTY + 2);
+    h_r = hy * kHX + hx;
+    h_px = hx ? h_r + kHX - 1 : kPhiCol + hy + 1;
+    const int hi_ = i0 - 1 + hx, hj = j0 - 1 + hy;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1) msk |= 1u << c;
+      if (tid < kHaloPts && hi_ >= 1 && hj >= 1 && hi_ < g.ext(c, 0) - 1 && hj < g.ext(c, 1) - 1) msk |= 8u << c;
+    }
+  }
+  constexpr int kOwn0 = kHX + 1;  // ring index of thread 0's own point; phi index kOwn0 + kHX
+  const int o_r = ty * kHX + tx + kOwn0;
+  float e0 = 0.f, e1 = 0.f, e2 = 0.f;  // the own point's exact residuals at the plane projected last
+  // Projection of ring plane kk: u' = fl(u + inc) at the interior points;
+  // with own_exact the own point's stored residual lo becomes lo + e (e0..e2).
+  auto two_sum_err = [](float a, float b, float s) {
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  };
+  auto project_plane = [&](int kk, bool own_exact) {
+    float *const rb = ring.f[0][kk & 3];
+    const float *const ph = ring.phi[kk & 3] + kHX, *const phb = ring.phi[(kk - 1) & 3] + kHX;
+    const unsigned kin = (kk >= 1) ? ((kk < lim0 ? 9u : 0u) | (kk < lim1 ? 18u : 0u) | (kk < lim2 ? 36u : 0u)) : 0u;
+    const unsigned m = msk & kin;
+    {
+      const float f0 = ph[o_r];
+      float lo0 = __bfloat162float(l0), lo1 = __bfloat162float(l1), lo2 = __bfloat162float(l2);
+      if (m & 1u) {
+        const float inc = -(((f0 - ph[o_r - 1]) * oh0) * pdt), hi = rb[o_r], s = __fadd_rn(hi, inc);
+        rb[o_r] = s;
+        lo0 = __fadd_rn(lo0, two_sum_err(hi, inc, s));
+      }
+      if (m & 2u) {
+        const float inc = -(((f0 - ph[o_r - kHX]) * oh1) * pdt), hi = rb[4 * kPL + o_r], s = __fadd_rn(hi, inc);
+        rb[4 * kPL + o_r] = s;
+        lo1 = __fadd_rn(lo1, two_sum_err(hi, inc, s));
+      }
+      if (m & 4u) {
+        const float inc = -(((f0 - phb[o_r]) * oh2) * pdt), hi = rb[8 * kPL + o_r], s = __fadd_rn(hi, inc);
+        rb[8 * kPL + o_r] = s;
+        lo2 = __fadd_rn(lo2, two_sum_err(hi, inc, s));
+      }
+      if (own_exact) e0 = lo0, e1 = lo1, e2 = lo2;
+    }
+    if (m & 0x38u) {
+      const float f0 = ph[h_r];
+      if (m & 8u) rb[h_r] = __fadd_rn(rb[h_r], -(((f0 - ring.phi[kk & 3][h_px]) * oh0) * pdt));
+      if (m & 16u) rb[4 * kPL + h_r] = __fadd_rn(rb[4 * kPL + h_r], -(((f0 - ph[h_r - kHX]) * oh1) * pdt));
+      if (m & 32u) rb[8 * kPL + h_r] = __fadd_rn(rb[8 * kPL + h_r], -(((f0 - phb[h_r]) * oh2) * pdt));
+    }
+  };
+  // p + phi, stochastically rounded with project_pair_kernel's draws
+  const unsigned psalt = sr_salt(tr, pj.tag);
+  auto p_new = [&](int r, int kk, long q) {
+    const unsigned h = sr_mix((unsigned)q ^ psalt);
+    return add_sr(ring.f[3][kk & 3][r], ring.phi[kk & 3][r + kHX], sr_draw(sr_mix(h), 0));
+  };
+  // Pressure nodes outside the threads' range, at the CTAs on those edges.
+  const int E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
+  const bool edge_x0 = blockIdx.x == 0, edge_y0 = blockIdx.y == 0, edge_xr = i0 + kTX == E0 - 1;
+  auto write_p_edges = [&](int kk) {
+    auto one = [&](int hx, int hy) {
+      const int pi = i0 - 1 + hx, pjj = j0 - 1 + hy;
+      if (pi >= E0 || pjj >= E1 || kk >= E2) return;
+      const long q = pi + PX * (pjj + g.PY * (long)kk);
+      p_out[q] = p_new(hy * kHX + hx, kk, q);
+    };
+    if (edge_x0 && tx == 0) one(0, ty + 1);
+    if (edge_xr && tx == kTX - 1) one(kTX + 1, ty + 1);
+    if (edge_y0 && ty == 0) {
+      one(tx + 1, 0);
+      if (edge_x0 && tx == 0) one(0, 0);
+      if (edge_xr && tx == kTX - 1) one(kTX + 1, 0);
+    }
+  };
+  const bool own_p = i < E0 && j < E1;
+  const bool edges = edge_x0 | edge_y0 | edge_xr;
+  // Prologue: phi of plane kbeg - 2 (w's projection of plane kbeg - 1), the
+  // planes kbeg - 1 .. kbeg + 1; planes kbeg - 1 and kbeg projected.
+  load_plane(kbeg - 2, true);
+  load_plane(kbeg - 1, false);
+  load_plane(kbeg, false);
+  load_plane(kbeg + 1, false);
+  cp_wait1();
+  __syncthreads();
+  project_plane(kbeg - 1, false);
+  prefetch(kbeg);
+  project_plane(kbeg, true);
+  if (kbeg == 1) {  // the pressure of plane 0, which no thread's march reaches
+    if (own_p) p_out[qij] = p_new(o_r, 0, qij);
+    if (edges) write_p_edges(0);
+  }
+  __syncthreads();  // the first iteration refills the slot of plane kbeg - 2
+  const float *const tap0 = &ring.f[0][0][o_r];
+  for (int k = kbeg; k < kend; ++k) {
+    load_plane(k + 2, false);
+    if (kForce) fz = fe.axis(2, k);
+    const float c0 = n0, c1 = n1, c2 = n2, lo0 = e0, lo1 = e1, lo2 = e2;
+    prefetch(k + 1);
+    cp_wait1();
+    __syncthreads();
+    project_plane(k + 1, true);
+    __syncthreads();
+    Tap<float> A;
+#pragma unroll
+    for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
+    const float *const ph = ring.phi[k & 3] + kHX, *const phb = ring.phi[(k - 1) & 3] + kHX;
+    const float f14 = ph[o_r];
+    const long q = qij + (long)k * plane;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (!((msk >> c) & 1u) || k >= (c == 0 ? lim0 : (c == 1 ? lim1 : lim2))) continue;
+      Taps<float> tp;
+      tp.load_c(A, c, true);
+      float r = rhs_taps(c, tp, co);
+      if (kForce) r = r + fe.eval(c, fx, fy, fz);
+      const float fb = c == 0 ? ph[o_r - 1] : (c == 1 ? ph[o_r - kHX] : phb[o_r]);
+      const float gp = (tp.dp(c) + (f14 - fb)) * (c == 0 ? oh0 : (c == 1 ? oh1 : oh2));
+      const float self = tp.self(c);
+      const float cur = c == 0 ? c0 : (c == 1 ? c1 : c2), lo = c == 0 ? lo0 : (c == 1 ? lo1 : lo2);
+      __nv_bfloat16 *lo_out = res.c[c] + q;
+      if constexpr (ST == kStageY3) {
+        const float r2s = K.k2 * r;
+        F.vel(2, c)[q] = comp_add(self, lo, K.k1 * cur + r2s - K.k3 * gp, lo_out);
+        F.vel(0, c)[q] = r2s;
+      } else {
+        F.vel(0, c)[q] = comp_add(self, lo, -cur + K.k2 * r - K.k3 * gp, lo_out);
+      }
+    }
+    if (own_p) p_out[q] = p_new(o_r, k, q);
+    if (edges) write_p_edges(k);
+    __syncthreads();  // the next iteration refills the slot of plane k - 1
+  }
+}
+
 // ---- boundary fill, src/VelocityTensor.cpp:36-233 ----
 
 // Sampling point of component c at index (i,j,k): staggered (face) along c.
@@ -1167,8 +1463,18 @@ struct StageLaunch {
   TimeRef tr;
   int sin_slot, kc;
   Residual res;
+  const StageProj *proj;
   template <int ST>
   void go(bool comp) const {
+    if constexpr (std::is_same<T, float>::value && (ST == kStageY3 || ST == kStageUStar)) {
+      if (comp && proj) {
+        if (forcing)
+          stage_proj_kernel<ST, true><<<grid, blk, 0, s>>>(g, co, F, K, fe, tr, sin_slot, kc, res, *proj);
+        else
+          stage_proj_kernel<ST, false><<<grid, blk, 0, s>>>(g, co, F, K, fe, tr, sin_slot, kc, res, *proj);
+        return;
+      }
+    }
     if constexpr (std::is_same<T, float>::value && ST <= kStageUStar) {
       if (comp) {
         stage_kernel_tiled<T, ST, true><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res);
@@ -1186,7 +1492,7 @@ struct StageLaunch {
 template <typename T>
 void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches,
-                  const Residual &res) {
+                  const Residual &res, const StageProj *proj) {
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
   const int nk = g.Es[2] - 2;
   // Planes per CTA: 32, halved (down to 4) while the grid would not fill the
@@ -1248,7 +1554,7 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   const Coeffs<T> co = make_coeffs<T>(g);
   const dim3 blk(kTX * kTY);
   const bool comp = res.on() && st <= kStageUStar;
-  const StageLaunch<T> L{tgrid, blk, s, g, co, F, K, forcing, fe, tr, sc.sin_slot, kc, res};
+  const StageLaunch<T> L{tgrid, blk, s, g, co, F, K, forcing, fe, tr, sc.sin_slot, kc, res, comp ? proj : nullptr};
   switch (st) {
     case kStageY2: L.template go<kStageY2>(comp); break;
     case kStageY3: L.template go<kStageY3>(comp); break;
@@ -1457,7 +1763,7 @@ void launch_pressure_gradient(const Geometry &g, T *const vel[3], const T *p, cu
 #define MIFGPU_INSTANTIATE(T)                                                                                        \
   template void launch_stage<T>(const Geometry &, const Fields<T> &, StageKind, const StageScalars<T> &,             \
                                 const ForcingTables<T> &, int, TimeRef, cudaStream_t, long long *,                   \
-                                const Residual &);                                                                   \
+                                const Residual &, const StageProj *);                                                \
   template void launch_apply_bc<T>(const Geometry &, T *const[3], int, int, TimeRef, int, const FaceTables &,     \
                                    cudaStream_t, long long *, const Residual &);                                  \
   template void launch_periodic_scalar<T>(const Geometry &, T *, cudaStream_t, long long *);                       \
