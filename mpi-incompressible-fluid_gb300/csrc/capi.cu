@@ -183,7 +183,9 @@ struct Impl final : ImplBase {
   double *slots = nullptr;  // device: kSlotSize doubles per step
   int slots_cap = 0;
   int *step_ctr = nullptr;  // device step index the graph reads and advances
-  int *nonfinite = nullptr; // device flag: a projection saw a NaN or Inf in phi
+  // device flags: [0] a projection saw a NaN or Inf in phi, [1] a stage
+  // kernel gave up waiting for a TMA tile load
+  int *nonfinite = nullptr;
   double *acc = nullptr;    // device reduction scratch
   double *staging = nullptr;
   size_t staging_elems = 0;
@@ -318,8 +320,8 @@ struct Impl final : ImplBase {
     if (int rc = init_face_tables(ctx)) return rc;
     CK(cudaMalloc(&step_ctr, sizeof(int)));
     CK(cudaMemset(step_ctr, 0, sizeof(int)));
-    CK(cudaMalloc(&nonfinite, sizeof(int)));
-    CK(cudaMemset(nonfinite, 0, sizeof(int)));
+    CK(cudaMalloc(&nonfinite, 2 * sizeof(int)));
+    CK(cudaMemset(nonfinite, 0, 2 * sizeof(int)));
     CK(cudaMalloc(&acc, sizeof(double) * 16));
     CK(alloc_slots());
     CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
@@ -624,23 +626,26 @@ struct Impl final : ImplBase {
     launch_project<T>(g, F.f[kP], F.f[kPhi], vel, dt, tref(), tag, s, cnt, r, watch);
   }
 
-  // The kernels of one step of the given variant, in stream order.
-  void enqueue_step(mifgpu_ctx *ctx, cudaStream_t s, int variant, long long *cnt) {
+  // The kernels of one step of the given variant, in stream order. False
+  // if a stage kernel could not be launched (its tensor maps were rejected).
+  bool enqueue_step(mifgpu_ctx *ctx, cudaStream_t s, int variant, long long *cnt) {
     const double dt = g.dt;
     ForcingTables<T> ft{ftab, ftab_maxE};
     const int kind = ctx->prm.boundary_kind;
+    int *const kerr = nonfinite + 1;
+    bool ok = true;
     if (variant == kVariantVelocity) {
       StageScalars<T> sc{dt, 4, 1, 0.0};
       const Residual none{};
-      launch_stage<T>(g, F, kVelY2, sc, ft, kind, tref(), s, cnt);
+      ok &= launch_stage<T>(g, F, kVelY2, sc, ft, kind, tref(), s, cnt, none, nullptr, kerr);
       enqueue_bc(ctx, s, 1, 1, cnt, none);
       sc.sin_slot = 6;
-      launch_stage<T>(g, F, kVelY3, sc, ft, kind, tref(), s, cnt);
+      ok &= launch_stage<T>(g, F, kVelY3, sc, ft, kind, tref(), s, cnt, none, nullptr, kerr);
       enqueue_bc(ctx, s, 0, 2, cnt, none);
       sc.sin_slot = 8;
-      launch_stage<T>(g, F, kVelUStar, sc, ft, kind, tref(), s, cnt);
+      ok &= launch_stage<T>(g, F, kVelUStar, sc, ft, kind, tref(), s, cnt, none, nullptr, kerr);
       enqueue_bc(ctx, s, 1, 3, cnt, none);
-      return;  // the final swap of sets 0 and 1 is done on the host side
+      return ok;  // the final swap of sets 0 and 1 is done on the host side
     }
     const bool nhn = variant == kVariantNhn;
     const double dts[3] = {64.0 / 120.0 * dt, 16.0 / 120.0 * dt, 40.0 / 120.0 * dt};
@@ -664,12 +669,14 @@ struct Impl final : ImplBase {
       }
       // in the compensated state every stage's output set carries the residuals
       mark(MIFGPU_PROF_STAGE, s);
-      launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res, fused && st > 0 ? &pj : nullptr);
+      ok &= launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res, fused && st > 0 ? &pj : nullptr,
+                            kerr);
       enqueue_bc(ctx, s, out_set[st], 1 + st, cnt, res);
       enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt, res);
       // the last projection of the step watches phi for NaN / Inf
       if (!fused || st == 2) enqueue_project(s, out_set[st], dts[st], 16u + st, cnt, res, st == 2 ? nonfinite : nullptr);
     }
+    return ok;
   }
 
   int ensure_graph(mifgpu_ctx *ctx, int variant) {
@@ -677,11 +684,15 @@ struct Impl final : ImplBase {
     cudaGraph_t gr = nullptr;
     CK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
     long long cnt = 0;
-    enqueue_step(ctx, cap_stream, variant, &cnt);
+    const bool launched = enqueue_step(ctx, cap_stream, variant, &cnt);
     advance_step_kernel<<<1, 1, 0, cap_stream>>>(step_ctr);
     ++cnt;
     cudaError_t e = cudaStreamEndCapture(cap_stream, &gr);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "stream capture of the step");
+    if (!launched) {
+      cudaGraphDestroy(gr);
+      return fail(ctx, MIFGPU_ECUDA, "cuTensorMapEncodeTiled rejected a stage kernel's tile map");
+    }
     e = cudaGraphInstantiate(&graph[variant][parity], gr, 0);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
@@ -701,7 +712,7 @@ struct Impl final : ImplBase {
       swap_sets();
       if (rc) return rc;
     }
-    CK(cudaMemsetAsync(nonfinite, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(nonfinite, 0, 2 * sizeof(int), ctx->stream));
     for (int n0 = 0; n0 < nsteps; n0 += slots_cap) {
       const int chunk = std::min(slots_cap, nsteps - n0);
       CK(cudaMemcpyAsync(slots, host_slots + (size_t)kSlotSize * n0, sizeof(double) * kSlotSize * chunk,
@@ -714,10 +725,11 @@ struct Impl final : ImplBase {
       }
     }
     // The host copy of the slots may be a temporary: wait until it was consumed.
-    int bad = 0;
-    CK(cudaMemcpyAsync(&bad, nonfinite, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    int bad[2] = {0, 0};
+    CK(cudaMemcpyAsync(bad, nonfinite, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    if (bad)
+    if (bad[1]) return fail(ctx, MIFGPU_ECUDA, "a stage kernel gave up waiting for a TMA tile load");
+    if (bad[0])
       return fail(ctx, MIFGPU_ENONFINITE,
                   "a projection step produced a NaN or Inf pressure increment (the velocity or pressure is no longer "
                   "finite)");
@@ -733,10 +745,14 @@ struct Impl final : ImplBase {
       std::vector<std::pair<int, cudaEvent_t>> marks;
       prof = &marks;
       CK(cudaMemsetAsync(step_ctr, 0, sizeof(int), ctx->stream));
-      enqueue_step(ctx, ctx->stream, kVariantProjection, &ctx->launches);
+      const bool launched = enqueue_step(ctx, ctx->stream, kVariantProjection, &ctx->launches);
       mark(-1, ctx->stream);
       prof = nullptr;
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (!launched) {
+        for (auto &m : marks) cudaEventDestroy(m.second);
+        return fail(ctx, MIFGPU_ECUDA, "cuTensorMapEncodeTiled rejected a stage kernel's tile map");
+      }
       for (size_t q = 0; q + 1 < marks.size(); ++q) {
         float t = 0.f;
         cudaEventElapsedTime(&t, marks[q].second, marks[q + 1].second);

@@ -94,11 +94,13 @@ struct StageProj {
 
 // `res`: the compensated state's residuals (projection stages, float only).
 // `proj` (compensated kStageY3 / kStageUStar only, or null): the preceding
-// projection, done inside the stage.
+// projection, done inside the stage. The plane ring is filled by TMA tile
+// loads; `kerr` (device, may be null) is set to 1 if a CTA gave up waiting
+// for one. Returns false (nothing launched) if a tensor map was rejected.
 template <typename T>
-void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
+bool launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches,
-                  const Residual &res = Residual{}, const StageProj *proj = nullptr);
+                  const Residual &res = Residual{}, const StageProj *proj = nullptr, int *kerr = nullptr);
 
 // Dirichlet faces (fn 0 velocity family, 1 pressure-gradient family) then the
 // periodic copies, on velocity set `set` (src/VelocityTensor.cpp:36-233).

@@ -15,6 +15,7 @@
 
 #include "analytic.cuh"
 #include "stencil.cuh"
+#include "tma.cuh"
 
 namespace mifgpu {
 
@@ -174,39 +175,19 @@ struct StageCoef {
 // A CTA owns a TX x TY tile of (i, j) and marches through kc planes of k. The
 // input velocity set and p live in a ring of four shared-memory planes per
 // field (k-1, k, k+1 and the plane being prefetched), each with a one-point
-// halo in x and y; plane k+2 is copied with cp.async while plane k is
-// computed. Every stencil neighbour of include/MomentumEquation.h then comes
-// from shared memory and each point costs about five global loads.
-// Tile rows hold kTX + 2 used elements at a pitch of kTX + 4, so every row
-// starts 16-byte aligned and is copied with 16-byte cp.async.
-constexpr int kTX = 32, kTY = 4, kHX = kTX + 4, kHY = kTY + 2, kPL = kHX * kHY;
-
-__device__ __forceinline__ void cp_async4_st(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async8_st(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async16_st(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
-}
-// One element of T (4 or 8 bytes) into shared memory.
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem) {
-  if constexpr (sizeof(T) == 8)
-    cp_async8_st(smem, gmem);
-  else
-    cp_async4_st(smem, gmem);
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+// halo in x and y; plane k+2 is loaded by TMA while plane k is computed.
+// Every stencil neighbour of include/MomentumEquation.h then comes from
+// shared memory and each point costs about five global loads. Tile rows hold
+// kTX + 2 used elements at a pitch of kTX + 4: a plane tile is one TMA box of
+// kHX x kHY elements. A TMA destination in shared memory starts 128-byte
+// aligned, so the ring slots are kSlot elements apart (the kPL-element tile
+// and padding; 896 bytes in float, 1792 in double).
+constexpr int kTX = 32, kTY = 4, kHX = kTX + 4, kHY = kTY + 2, kPL = kHX * kHY, kSlot = 224;
+static_assert(kSlot >= kPL && (kSlot * 4) % 128 == 0, "128-byte aligned ring slots");
 
 template <typename T>
 struct Ring {
-  T f[4][4][kPL];  // field (u, v, w, p), slot (k & 3), tile
+  T f[4][4][kSlot];  // field (u, v, w, p), slot (k & 3), tile
 };
 
 // Neighbour accessor on the ring: field f at (i + di, j + dj, k + dk).
@@ -217,7 +198,7 @@ struct Tap {
   // plus a compile-time offset.
   const T *pl[3];
   __device__ __forceinline__ T operator()(int f, int di, int dj, int dk) const {
-    return pl[dk + 1][f * 4 * kPL + dj * kHX + di];
+    return pl[dk + 1][f * 4 * kSlot + dj * kHX + di];
   }
 };
 
@@ -311,12 +292,12 @@ template <typename T, int ST, bool kComp>
 __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinBlocksComp : kStageMinBlocksF32)
                                                            : kStageMinBlocksF64)
     stage_kernel_tiled(Geometry g, Coeffs<T> co, Fields<T> F, StageCoef<T> K, int forcing, ForcingEval<T> fe,
-                       TimeRef tr, int sin_slot, int kc, Residual res) {
+                       TimeRef tr, int sin_slot, int kc, Residual res, const __grid_constant__ StageMaps maps,
+                       int *kerr) {
+  // maps.m[0..2]: the input set's u, v, w (set 0 for Y2 and the velocity-only
+  // Y2 and U*, set 1 for Y3, set 2 for U* and the velocity-only Y3), m[3]: p
   constexpr bool kUseP = ST == kStageY2 || ST == kStageY3 || ST == kStageUStar;
-  constexpr int in_set = (ST == kStageY2 || ST == kVelY2 || ST == kVelUStar) ? 0
-                         : (ST == kStageY3 || ST == kVelY3)                  ? 1
-                                                                             : 2;
-  __shared__ __align__(16) Ring<T> ring;
+  __shared__ __align__(128) Ring<T> ring;
   if (forcing) {
     fe.st = T(tr.get(sin_slot));
     fe.ct = T(tr.get(sin_slot + 1));
@@ -326,48 +307,45 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
   const int i0 = 1 + blockIdx.x * kTX, j0 = 1 + blockIdx.y * kTY;
   const int zmax = g.Es[2] - 1;  // interior k < zmax
   const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
-  const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
   constexpr int nf = kUseP ? 4 : 3;
-  // A tile row starts at x = i0 - 1 = 32 * blockIdx.x (16-byte aligned, PX a
-  // multiple of 8) and is copied as kHX / kVec vectors of 16 bytes; vectors
-  // outside the box are zero-filled. Only the first kTX + 2 of a row are read.
-  constexpr int kVec = 16 / sizeof(T), kVecRow = kHX / kVec, kVecPlane = kVecRow * kHY;
-  constexpr int kVecPer = (kVecPlane * 4 + kTX * kTY - 1) / (kTX * kTY);  // vectors per thread and plane
-  // This thread's tile vectors, fixed for every plane: shared-memory offset
-  // within a slot (-1: none), source pointer and in-plane offset (-1: outside
-  // the box, zero-filled).
-  int v_sm[kVecPer];
-  const T *v_src[kVecPer];
-  long v_off[kVecPer];
+  // The ring is filled by TMA: thread 0 loads plane kk's nf tiles (36 x 6
+  // elements from (i0 - 1, j0 - 1), i0 - 1 = 32 * blockIdx.x, 16-byte
+  // aligned as PX is a multiple of 8; zeros outside the box) into slot
+  // kk & 3 on that slot's mbarrier, and every thread waits on the barrier
+  // before reading the plane. Plane kk is the ((kk - kfirst) / 4)-th load of
+  // its slot, which fixes the phase to wait for.
+  __shared__ uint64_t bars[4];
+  const int kfirst = kbeg - 1;
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int r = 0; r < kVecPer; ++r) {
-    const int e = threadIdx.x + r * kTX * kTY;
-    const int f = e / kVecPlane, ev = e - f * kVecPlane;
-    const int hy = ev / kVecRow, hx = (ev - hy * kVecRow) * kVec;
-    const int i = i0 - 1 + hx, j = j0 - 1 + hy;
-    v_sm[r] = f < nf ? (int)(&ring.f[f][0][hy * kHX + hx] - &ring.f[0][0][0]) : -1;
-    v_src[r] = f == 0 ? src[0] : (f == 1 ? src[1] : (f == 2 ? src[2] : src[3]));
-    v_off[r] = (i < g.PX && j < g.PY) ? (long)i + g.PX * (long)j : -1;
+    for (int b = 0; b < 4; ++b) mbar_init(&bars[b], 1);
+    mbar_init_fence();
   }
-  const long plane = g.sz();
-  T *const ring0 = &ring.f[0][0][0];
-  auto load_plane = [&](int kk) {
+  __syncthreads();
+  auto load_plane = [&](int kk) {  // thread 0
+    uint64_t *bar = &bars[kk & 3];
     if (kk >= 0 && kk < g.PZ) {
+      mbar_expect_tx(bar, (unsigned)(nf * kPL * sizeof(T)));
 #pragma unroll
-      for (int r = 0; r < kVecPer; ++r) {
-        if (v_sm[r] < 0) continue;
-        T *d = ring0 + v_sm[r] + (kk & 3) * kPL;
-        if (v_off[r] >= 0)
-          cp_async16_st(d, v_src[r] + v_off[r] + kk * plane);
-        else
-          *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
+      for (int f = 0; f < nf; ++f) tma_load_3d(&ring.f[f][kk & 3][0], &maps.m[f], i0 - 1, j0 - 1, kk, bar);
+    } else {
+      mbar_arrive(bar);
     }
-    cp_commit();
   };
-  load_plane(kbeg - 1);
-  load_plane(kbeg);
-  load_plane(kbeg + 1);
+  // A wait that gives up records it in *kerr; later waits of the thread are
+  // skipped, so a CTA always runs to its end.
+  bool tma_ok = true;
+  auto wait_plane = [&](int kk) {
+    if (tma_ok && !mbar_wait(&bars[kk & 3], ((kk - kfirst) >> 2) & 1)) {
+      tma_ok = false;
+      if (kerr) atomicExch(kerr, 1);
+    }
+  };
+  if (threadIdx.x == 0) {
+    load_plane(kbeg - 1);
+    load_plane(kbeg);
+    load_plane(kbeg + 1);
+  }
   const int i = i0 + tx, j = j0 + ty;
   const long sy = g.sy(), sz = g.sz();
   const T *const tap0 = &ring.f[0][0][(ty + 1) * kHX + tx + 1];
@@ -407,8 +385,15 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
     klim[c] = g.ext(c, 2) - 1;
   }
   const long qij = (long)i + g.PX * (long)j;
+  wait_plane(kbeg - 1);
+  wait_plane(kbeg);
   for (int k = kbeg; k < kend; ++k) {
-    load_plane(k + 2);
+    // plane k + 2 into the slot of plane k - 2, which the barrier that ended
+    // the previous iteration released
+    if (threadIdx.x == 0 && k + 2 <= kend) {
+      fence_async_shared();
+      load_plane(k + 2);
+    }
     if (forcing) fz = fe.axis(2, k);
     T c2[3], c0[3];
     __nv_bfloat16 cl[3];
@@ -419,11 +404,10 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
       cl[c] = nl[c];
     }
     prefetch(k + 1);
-    cp_wait1();
-    __syncthreads();
+    wait_plane(k + 1);
     Tap<T> A;
 #pragma unroll
-    for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
+    for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kSlot;
     const long q = qij + (long)k * sz;
     const unsigned hq = std::is_same<T, float>::value ? sr_mix((unsigned)q ^ salt) : 0u;
 #pragma unroll
@@ -516,12 +500,13 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
 // (x = 0, y = 0, z = 0 and the last x node of a periodic axis when it falls on
 // the tile halo) are written by the CTAs at those edges.
 
-// phi tile: rows j0 - 2 .. j0 + kTY (kTY + 3), columns x = i0 - 1 .. i0 + 34 at
-// the velocity tiles' pitch, then the column x = i0 - 2 (one value per row).
-constexpr int kPhiRows = kTY + 3, kPhiCol = kHX * kPhiRows, kPhiPL = kPhiCol + 8;
+// phi tile: one TMA box of kPhiX x kPhiRows from (i0 - 5, j0 - 2), 16-byte
+// aligned in x: ring point (hx, hy) is phi element (hx + 4, hy + 1).
+constexpr int kPhiRows = kTY + 3, kPhiX = kHX + 4, kPhiPL = kPhiX * kPhiRows, kPhiSlot = 288;
+static_assert(kPhiSlot >= kPhiPL && (kPhiSlot * 4) % 128 == 0, "128-byte aligned phi slots");
 struct RingProj {
-  float f[4][4][kPL];  // u, v, w, p: slot (k & 3), as Ring
-  float phi[4][kPhiPL];
+  float f[4][4][kSlot];  // u, v, w, p: slot (k & 3), as Ring
+  float phi[4][kPhiSlot];
 };
 // The ring points (hx, hy) outside the CTA's own kTX x kTY: rows hy = 0 and
 // kTY + 1 (hx = 1 .. kTX), then columns hx = 0 and kTX + 1 (hy = 0 .. kTY + 1).
@@ -540,10 +525,12 @@ constexpr int kStageProjMinBlocks = MIFGPU_STAGE_PROJ_BLOCKS;
 template <int ST, bool kForce>
 __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
     stage_proj_kernel(Geometry g, Coeffs<float> co, Fields<float> F, StageCoef<float> K, ForcingEval<float> fe,
-                      TimeRef tr, int sin_slot, int kc, Residual res, StageProj pj) {
+                      TimeRef tr, int sin_slot, int kc, Residual res, StageProj pj,
+                      const __grid_constant__ StageMaps maps, int *kerr) {
   static_assert(ST == kStageY3 || ST == kStageUStar, "the stages that follow a projection");
-  constexpr int in_set = ST == kStageY3 ? 1 : 2, oth_set = ST == kStageY3 ? 2 : 0;
-  __shared__ __align__(16) RingProj ring;
+  constexpr int oth_set = ST == kStageY3 ? 2 : 0;
+  __shared__ __align__(128) RingProj ring;
+  __shared__ uint64_t bars[4];
   if (kForce) {
     fe.st = float(tr.get(sin_slot));
     fe.ct = float(tr.get(sin_slot + 1));
@@ -554,66 +541,40 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   const int PZ = (int)g.PZ;
   const int lim0 = g.ext(0, 2) - 1, lim1 = g.ext(1, 2) - 1, lim2 = g.ext(2, 2) - 1;
   const float pdt = pj.dt, oh0 = co.oh[0], oh1 = co.oh[1], oh2 = co.oh[2];
-  const float *const phi_g = pj.phi;
   float *const p_out = pj.p_out;
   const int tid = threadIdx.x, tx = tid % kTX, ty = tid / kTX;
   const int i0 = 1 + blockIdx.x * kTX, j0 = 1 + blockIdx.y * kTY;
   const int zmax = g.Es[2] - 1;  // interior k < zmax
   const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
-  // Plane loads (16-byte vectors): threads t and 64 + t (t < 54) copy vector
-  // t of the u, w tiles and of the v, p tiles; threads t < 63 vector t of the
-  // phi tile; the last kPhiRows threads the phi column x = i0 - 2 (4 bytes).
-  // Shared offsets relative to the slot, source offsets within the plane (-1:
-  // a zero vector).
-  constexpr int kVecRow = kHX / 4, kVecPlane = kVecRow * kHY, kVecPhi = kVecRow * kPhiRows;
-  const int vt = tid & 63, half = tid >> 6;
-  int va = -1, va_off = -1, vp = -1, vp_off = -1;
-  if (vt < kVecPlane) {
-    const int hy = vt / kVecRow, hx = (vt - hy * kVecRow) * 4, ii = i0 - 1 + hx, jj = j0 - 1 + hy;
-    va = hy * kHX + hx;
-    va_off = (ii < PX && jj < g.PY) ? ii + (int)PX * jj : -1;
+  // TMA ring fill (as stage_kernel_tiled): maps 0..3 the input set's u, v, w
+  // and p_in (kHX x kHY boxes from (i0 - 1, j0 - 1)), map 4 phi (kPhiX x
+  // kPhiRows from (i0 - 5, j0 - 2)); thread 0 loads, every thread waits on the
+  // slot's mbarrier. The first load is phi alone, of plane kbeg - 2.
+  const int kfirst = kbeg - 2;
+  if (tid == 0) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) mbar_init(&bars[b], 1);
+    mbar_init_fence();
   }
-  if (tid < kVecPhi) {
-    const int row = tid / kVecRow, hx = (tid - row * kVecRow) * 4, ii = i0 - 1 + hx, jj = j0 - 2 + row;
-    vp = row * kHX + hx;
-    vp_off = (jj >= 0 && ii < PX && jj < g.PY) ? ii + (int)PX * jj : -1;
-  } else if (tid >= kTX * kTY - kPhiRows) {
-    const int row = tid - (kTX * kTY - kPhiRows), ii = i0 - 2, jj = j0 - 2 + row;
-    vp = kPhiCol + row;
-    vp_off = (ii >= 0 && jj >= 0 && jj < g.PY) ? ii + (int)PX * jj : -1;
-  }
-  const float *const src_a = F.f[in_set * kFieldsPerSet + half];
-  const float *const src_b = half ? pj.p_in : F.f[in_set * kFieldsPerSet + 2];
-  auto load_plane = [&](int kk, bool phi_only) {
+  __syncthreads();
+  auto load_plane = [&](int kk, bool phi_only) {  // thread 0
+    uint64_t *bar = &bars[kk & 3];
     if (kk >= 0 && kk < PZ) {
-      const long po = (long)kk * plane;
-      const int sl = kk & 3;
-      if (!phi_only && va >= 0) {
-        float *d0 = &ring.f[half][sl][va], *d1 = &ring.f[2 + half][sl][va];
-        if (va_off >= 0) {
-          cp_async16_st(d0, src_a + po + va_off);
-          cp_async16_st(d1, src_b + po + va_off);
-        } else {
-          *reinterpret_cast<float4 *>(d0) = make_float4(0.f, 0.f, 0.f, 0.f);
-          *reinterpret_cast<float4 *>(d1) = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-      }
-      if (vp >= 0) {
-        float *d = &ring.phi[sl][vp];
-        if (vp < kPhiCol) {
-          if (vp_off >= 0)
-            cp_async16_st(d, phi_g + po + vp_off);
-          else
-            *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
-        } else {
-          if (vp_off >= 0)
-            cp_async4_st(d, phi_g + po + vp_off);
-          else
-            *d = 0.f;
-        }
-      }
+      mbar_expect_tx(bar, (unsigned)(sizeof(float) * (kPhiPL + (phi_only ? 0 : 4 * kPL))));
+      if (!phi_only)
+#pragma unroll
+        for (int f = 0; f < 4; ++f) tma_load_3d(&ring.f[f][kk & 3][0], &maps.m[f], i0 - 1, j0 - 1, kk, bar);
+      tma_load_3d(&ring.phi[kk & 3][0], &maps.m[4], i0 - 5, j0 - 2, kk, bar);
+    } else {
+      mbar_arrive(bar);
     }
-    cp_commit();
+  };
+  bool tma_ok = true;
+  auto wait_plane = [&](int kk) {
+    if (tma_ok && !mbar_wait(&bars[kk & 3], ((kk - kfirst) >> 2) & 1)) {
+      tma_ok = false;
+      if (kerr) atomicExch(kerr, 1);
+    }
   };
   const int i = i0 + tx, j = j0 + ty;
   typename ForcingEval<float>::Axis fx{}, fy{}, fz{};
@@ -642,8 +603,8 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   };
   // Interior masks in x and y of the own point (bits 0-2: component) and of
   // this thread's halo point (bits 3-5; threads < kHaloPts), whose ring index
-  // is h_r (the phi index is h_r + kHX, one row down in the phi tile).
-  int h_r = 0, h_px = 0;  // h_px: phi index one point back in x (the phi column for hx = 0)
+  // is h_r and phi index h_p.
+  int h_r = 0, h_p = 0;
   unsigned msk = 0;
   {
     int hx = 0, hy = 0;
@@ -652,7 +613,7 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
     else if (tid < 2 * kTX + kTY + 2) hx = 0, hy = tid - 2 * kTX;
     else hx = kTX + 1, hy = tid - 2 * kTX - (kTY + 2);
     h_r = hy * kHX + hx;
-    h_px = hx ? h_r + kHX - 1 : kPhiCol + hy + 1;
+    h_p = (hy + 1) * kPhiX + hx + 4;
     const int hi_ = i0 - 1 + hx, hj = j0 - 1 + hy;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -660,8 +621,7 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
       if (tid < kHaloPts && hi_ >= 1 && hj >= 1 && hi_ < g.ext(c, 0) - 1 && hj < g.ext(c, 1) - 1) msk |= 8u << c;
     }
   }
-  constexpr int kOwn0 = kHX + 1;  // ring index of thread 0's own point; phi index kOwn0 + kHX
-  const int o_r = ty * kHX + tx + kOwn0;
+  const int o_r = (ty + 1) * kHX + tx + 1, o_p = (ty + 2) * kPhiX + tx + 5;  // own ring / phi index
   float e0 = 0.f, e1 = 0.f, e2 = 0.f;  // the own point's exact residuals at the plane projected last
   // Projection of ring plane kk: u' = fl(u + inc) at the interior points;
   // with own_exact the own point's stored residual lo becomes lo + e (e0..e2).
@@ -671,41 +631,41 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   };
   auto project_plane = [&](int kk, bool own_exact) {
     float *const rb = ring.f[0][kk & 3];
-    const float *const ph = ring.phi[kk & 3] + kHX, *const phb = ring.phi[(kk - 1) & 3] + kHX;
+    const float *const ph = ring.phi[kk & 3], *const phb = ring.phi[(kk - 1) & 3];
     const unsigned kin = (kk >= 1) ? ((kk < lim0 ? 9u : 0u) | (kk < lim1 ? 18u : 0u) | (kk < lim2 ? 36u : 0u)) : 0u;
     const unsigned m = msk & kin;
     {
-      const float f0 = ph[o_r];
+      const float f0 = ph[o_p];
       float lo0 = __bfloat162float(l0), lo1 = __bfloat162float(l1), lo2 = __bfloat162float(l2);
       if (m & 1u) {
-        const float inc = -(((f0 - ph[o_r - 1]) * oh0) * pdt), hi = rb[o_r], s = __fadd_rn(hi, inc);
+        const float inc = -(((f0 - ph[o_p - 1]) * oh0) * pdt), hi = rb[o_r], s = __fadd_rn(hi, inc);
         rb[o_r] = s;
         lo0 = __fadd_rn(lo0, two_sum_err(hi, inc, s));
       }
       if (m & 2u) {
-        const float inc = -(((f0 - ph[o_r - kHX]) * oh1) * pdt), hi = rb[4 * kPL + o_r], s = __fadd_rn(hi, inc);
-        rb[4 * kPL + o_r] = s;
+        const float inc = -(((f0 - ph[o_p - kPhiX]) * oh1) * pdt), hi = rb[4 * kSlot + o_r], s = __fadd_rn(hi, inc);
+        rb[4 * kSlot + o_r] = s;
         lo1 = __fadd_rn(lo1, two_sum_err(hi, inc, s));
       }
       if (m & 4u) {
-        const float inc = -(((f0 - phb[o_r]) * oh2) * pdt), hi = rb[8 * kPL + o_r], s = __fadd_rn(hi, inc);
-        rb[8 * kPL + o_r] = s;
+        const float inc = -(((f0 - phb[o_p]) * oh2) * pdt), hi = rb[8 * kSlot + o_r], s = __fadd_rn(hi, inc);
+        rb[8 * kSlot + o_r] = s;
         lo2 = __fadd_rn(lo2, two_sum_err(hi, inc, s));
       }
       if (own_exact) e0 = lo0, e1 = lo1, e2 = lo2;
     }
     if (m & 0x38u) {
-      const float f0 = ph[h_r];
-      if (m & 8u) rb[h_r] = __fadd_rn(rb[h_r], -(((f0 - ring.phi[kk & 3][h_px]) * oh0) * pdt));
-      if (m & 16u) rb[4 * kPL + h_r] = __fadd_rn(rb[4 * kPL + h_r], -(((f0 - ph[h_r - kHX]) * oh1) * pdt));
-      if (m & 32u) rb[8 * kPL + h_r] = __fadd_rn(rb[8 * kPL + h_r], -(((f0 - phb[h_r]) * oh2) * pdt));
+      const float f0 = ph[h_p];
+      if (m & 8u) rb[h_r] = __fadd_rn(rb[h_r], -(((f0 - ph[h_p - 1]) * oh0) * pdt));
+      if (m & 16u) rb[4 * kSlot + h_r] = __fadd_rn(rb[4 * kSlot + h_r], -(((f0 - ph[h_p - kPhiX]) * oh1) * pdt));
+      if (m & 32u) rb[8 * kSlot + h_r] = __fadd_rn(rb[8 * kSlot + h_r], -(((f0 - phb[h_p]) * oh2) * pdt));
     }
   };
   // p + phi, stochastically rounded with project_pair_kernel's draws
   const unsigned psalt = sr_salt(tr, pj.tag);
-  auto p_new = [&](int r, int kk, long q) {
+  auto p_new = [&](int r, int rp, int kk, long q) {
     const unsigned h = sr_mix((unsigned)q ^ psalt);
-    return add_sr(ring.f[3][kk & 3][r], ring.phi[kk & 3][r + kHX], sr_draw(sr_mix(h), 0));
+    return add_sr(ring.f[3][kk & 3][r], ring.phi[kk & 3][rp], sr_draw(sr_mix(h), 0));
   };
   // Pressure nodes outside the threads' range, at the CTAs on those edges.
   const int E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
@@ -715,7 +675,7 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
       const int pi = i0 - 1 + hx, pjj = j0 - 1 + hy;
       if (pi >= E0 || pjj >= E1 || kk >= E2) return;
       const long q = pi + PX * (pjj + g.PY * (long)kk);
-      p_out[q] = p_new(hy * kHX + hx, kk, q);
+      p_out[q] = p_new(hy * kHX + hx, (hy + 1) * kPhiX + hx + 4, kk, q);
     };
     if (edge_x0 && tx == 0) one(0, ty + 1);
     if (edge_xr && tx == kTX - 1) one(kTX + 1, ty + 1);
@@ -729,35 +689,40 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   const bool edges = edge_x0 | edge_y0 | edge_xr;
   // Prologue: phi of plane kbeg - 2 (w's projection of plane kbeg - 1), the
   // planes kbeg - 1 .. kbeg + 1; planes kbeg - 1 and kbeg projected.
-  load_plane(kbeg - 2, true);
-  load_plane(kbeg - 1, false);
-  load_plane(kbeg, false);
-  load_plane(kbeg + 1, false);
-  cp_wait1();
-  __syncthreads();
+  if (tid == 0) {
+    load_plane(kbeg - 2, true);
+    load_plane(kbeg - 1, false);
+    load_plane(kbeg, false);
+    load_plane(kbeg + 1, false);
+  }
+  wait_plane(kbeg - 2);
+  wait_plane(kbeg - 1);
+  wait_plane(kbeg);
   project_plane(kbeg - 1, false);
   prefetch(kbeg);
   project_plane(kbeg, true);
   if (kbeg == 1) {  // the pressure of plane 0, which no thread's march reaches
-    if (own_p) p_out[qij] = p_new(o_r, 0, qij);
+    if (own_p) p_out[qij] = p_new(o_r, o_p, 0, qij);
     if (edges) write_p_edges(0);
   }
   __syncthreads();  // the first iteration refills the slot of plane kbeg - 2
   const float *const tap0 = &ring.f[0][0][o_r];
   for (int k = kbeg; k < kend; ++k) {
-    load_plane(k + 2, false);
+    if (tid == 0 && k + 2 <= kend) {
+      fence_async_shared();
+      load_plane(k + 2, false);
+    }
     if (kForce) fz = fe.axis(2, k);
     const float c0 = n0, c1 = n1, c2 = n2, lo0 = e0, lo1 = e1, lo2 = e2;
     prefetch(k + 1);
-    cp_wait1();
-    __syncthreads();
+    wait_plane(k + 1);
     project_plane(k + 1, true);
     __syncthreads();
     Tap<float> A;
 #pragma unroll
-    for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kPL;
-    const float *const ph = ring.phi[k & 3] + kHX, *const phb = ring.phi[(k - 1) & 3] + kHX;
-    const float f14 = ph[o_r];
+    for (int dk = -1; dk <= 1; ++dk) A.pl[dk + 1] = tap0 + ((k + dk) & 3) * kSlot;
+    const float *const ph = ring.phi[k & 3], *const phb = ring.phi[(k - 1) & 3];
+    const float f14 = ph[o_p];
     const long q = qij + (long)k * plane;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -766,7 +731,7 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
       tp.load_c(A, c, true);
       float r = rhs_taps(c, tp, co);
       if (kForce) r = r + fe.eval(c, fx, fy, fz);
-      const float fb = c == 0 ? ph[o_r - 1] : (c == 1 ? ph[o_r - kHX] : phb[o_r]);
+      const float fb = c == 0 ? ph[o_p - 1] : (c == 1 ? ph[o_p - kPhiX] : phb[o_p]);
       const float gp = (tp.dp(c) + (f14 - fb)) * (c == 0 ? oh0 : (c == 1 ? oh1 : oh2));
       const float self = tp.self(c);
       const float cur = c == 0 ? c0 : (c == 1 ? c1 : c2), lo = c == 0 ? lo0 : (c == 1 ? lo1 : lo2);
@@ -779,7 +744,7 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
         F.vel(0, c)[q] = comp_add(self, lo, -cur + K.k2 * r - K.k3 * gp, lo_out);
       }
     }
-    if (own_p) p_out[q] = p_new(o_r, k, q);
+    if (own_p) p_out[q] = p_new(o_r, o_p, k, q);
     if (edges) write_p_edges(k);
     __syncthreads();  // the next iteration refills the slot of plane k - 1
   }
@@ -1464,24 +1429,42 @@ struct StageLaunch {
   int sin_slot, kc;
   Residual res;
   const StageProj *proj;
+  int *kerr;
+  // The tensor maps of the ring fields: the input set's u, v, w and p (the
+  // projecting stages' p_in), and phi for the projecting stages.
+  bool maps_for(int in_set, bool with_phi, StageMaps &m) const {
+    const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
+    if (proj) src[3] = reinterpret_cast<const T *>(proj->p_in);
+    for (int f = 0; f < 4; ++f)
+      if (!make_field_map(&m.m[f], src[f], (int)sizeof(T), g.PX, g.PY, g.PZ, kHX, kHY)) return false;
+    m.m[4] = m.m[3];
+    return !with_phi || make_field_map(&m.m[4], proj->phi, (int)sizeof(float), g.PX, g.PY, g.PZ, kPhiX, kPhiRows);
+  }
   template <int ST>
-  void go(bool comp) const {
+  bool go(bool comp) const {
+    constexpr int in_set = (ST == kStageY2 || ST == kVelY2 || ST == kVelUStar) ? 0
+                           : (ST == kStageY3 || ST == kVelY3)                  ? 1
+                                                                               : 2;
+    StageMaps m;
     if constexpr (std::is_same<T, float>::value && (ST == kStageY3 || ST == kStageUStar)) {
       if (comp && proj) {
+        if (!maps_for(in_set, true, m)) return false;
         if (forcing)
-          stage_proj_kernel<ST, true><<<grid, blk, 0, s>>>(g, co, F, K, fe, tr, sin_slot, kc, res, *proj);
+          stage_proj_kernel<ST, true><<<grid, blk, 0, s>>>(g, co, F, K, fe, tr, sin_slot, kc, res, *proj, m, kerr);
         else
-          stage_proj_kernel<ST, false><<<grid, blk, 0, s>>>(g, co, F, K, fe, tr, sin_slot, kc, res, *proj);
-        return;
+          stage_proj_kernel<ST, false><<<grid, blk, 0, s>>>(g, co, F, K, fe, tr, sin_slot, kc, res, *proj, m, kerr);
+        return true;
       }
     }
+    if (!maps_for(in_set, false, m)) return false;
     if constexpr (std::is_same<T, float>::value && ST <= kStageUStar) {
       if (comp) {
-        stage_kernel_tiled<T, ST, true><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res);
-        return;
+        stage_kernel_tiled<T, ST, true><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res, m, kerr);
+        return true;
       }
     }
-    stage_kernel_tiled<T, ST, false><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res);
+    stage_kernel_tiled<T, ST, false><<<grid, blk, 0, s>>>(g, co, F, K, forcing, fe, tr, sin_slot, kc, res, m, kerr);
+    return true;
   }
 };
 
@@ -1490,9 +1473,9 @@ struct StageLaunch {
 // ---- launchers ----
 
 template <typename T>
-void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
+bool launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const StageScalars<T> &sc,
                   const ForcingTables<T> &ft, int field_kind, TimeRef tr, cudaStream_t s, long long *launches,
-                  const Residual &res, const StageProj *proj) {
+                  const Residual &res, const StageProj *proj, int *kerr) {
   const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];  // widest extent per axis
   const int nk = g.Es[2] - 2;
   // Planes per CTA: 32, halved (down to 4) while the grid would not fill the
@@ -1554,16 +1537,19 @@ void launch_stage(const Geometry &g, const Fields<T> &F, StageKind st, const Sta
   const Coeffs<T> co = make_coeffs<T>(g);
   const dim3 blk(kTX * kTY);
   const bool comp = res.on() && st <= kStageUStar;
-  const StageLaunch<T> L{tgrid, blk, s, g, co, F, K, forcing, fe, tr, sc.sin_slot, kc, res, comp ? proj : nullptr};
+  const StageLaunch<T> L{tgrid, blk, s, g, co, F, K, forcing, fe, tr, sc.sin_slot, kc, res, comp ? proj : nullptr,
+                         kerr};
+  bool ok = false;
   switch (st) {
-    case kStageY2: L.template go<kStageY2>(comp); break;
-    case kStageY3: L.template go<kStageY3>(comp); break;
-    case kStageUStar: L.template go<kStageUStar>(comp); break;
-    case kVelY2: L.template go<kVelY2>(false); break;
-    case kVelY3: L.template go<kVelY3>(false); break;
-    default: L.template go<kVelUStar>(false); break;
+    case kStageY2: ok = L.template go<kStageY2>(comp); break;
+    case kStageY3: ok = L.template go<kStageY3>(comp); break;
+    case kStageUStar: ok = L.template go<kStageUStar>(comp); break;
+    case kVelY2: ok = L.template go<kVelY2>(false); break;
+    case kVelY3: ok = L.template go<kVelY3>(false); break;
+    default: ok = L.template go<kVelUStar>(false); break;
   }
-  if (launches) ++*launches;
+  if (ok && launches) ++*launches;
+  return ok;
 }
 
 template <typename T>
@@ -1761,9 +1747,9 @@ void launch_pressure_gradient(const Geometry &g, T *const vel[3], const T *p, cu
 }
 
 #define MIFGPU_INSTANTIATE(T)                                                                                        \
-  template void launch_stage<T>(const Geometry &, const Fields<T> &, StageKind, const StageScalars<T> &,             \
+  template bool launch_stage<T>(const Geometry &, const Fields<T> &, StageKind, const StageScalars<T> &,             \
                                 const ForcingTables<T> &, int, TimeRef, cudaStream_t, long long *,                   \
-                                const Residual &, const StageProj *);                                                \
+                                const Residual &, const StageProj *, int *);                                         \
   template void launch_apply_bc<T>(const Geometry &, T *const[3], int, int, TimeRef, int, const FaceTables &,     \
                                    cudaStream_t, long long *, const Residual &);                                  \
   template void launch_periodic_scalar<T>(const Geometry &, T *, cudaStream_t, long long *);                       \
