@@ -183,8 +183,8 @@ struct Impl final : ImplBase {
   double *slots = nullptr;  // device: kSlotSize doubles per step
   int slots_cap = 0;
   int *step_ctr = nullptr;  // device step index the graph reads and advances
-  // device flags: [0] a projection saw a NaN or Inf in phi, [1] a stage
-  // kernel gave up waiting for a TMA tile load
+  // device flags: [0] a projection saw a NaN or Inf in phi, [1] a stage or
+  // line kernel gave up waiting for a TMA tile load
   int *nonfinite = nullptr;
   double *acc = nullptr;    // device reduction scratch
   double *staging = nullptr;
@@ -322,6 +322,7 @@ struct Impl final : ImplBase {
     CK(cudaMemset(step_ctr, 0, sizeof(int)));
     CK(cudaMalloc(&nonfinite, 2 * sizeof(int)));
     CK(cudaMemset(nonfinite, 0, 2 * sizeof(int)));
+    ps.err_flag = nonfinite + 1;
     CK(cudaMalloc(&acc, sizeof(double) * 16));
     CK(alloc_slots());
     CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
@@ -728,7 +729,7 @@ struct Impl final : ImplBase {
     int bad[2] = {0, 0};
     CK(cudaMemcpyAsync(bad, nonfinite, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    if (bad[1]) return fail(ctx, MIFGPU_ECUDA, "a stage kernel gave up waiting for a TMA tile load");
+    if (bad[1]) return fail(ctx, MIFGPU_ECUDA, "a stage or line kernel gave up waiting for a TMA tile load");
     if (bad[0])
       return fail(ctx, MIFGPU_ENONFINITE,
                   "a projection step produced a NaN or Inf pressure increment (the velocity or pressure is no longer "

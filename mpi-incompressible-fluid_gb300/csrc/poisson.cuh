@@ -41,6 +41,7 @@ struct PoissonSolver {
   Geometry geo{};
   AxisPlan<T> axis[3];
   T *eig = nullptr;  // 1/(lambda sum) on the owner block, x fastest; 0 at the zero mode
+  int *err_flag = nullptr;  // device: set to 1 if a line kernel gave up waiting for its TMA loads
 
   int init(const Geometry &g, std::string &err);
   void release();

@@ -32,6 +32,7 @@
 #include "fft.cuh"
 #include "poisson.cuh"
 #include "regfft.cuh"
+#include "tma.cuh"
 
 namespace mifgpu {
 
@@ -76,6 +77,14 @@ struct LineArgs {
   int vec16;              // x lines, register path, half-length DCT-I: 0, or the row pitch (floats)
                           // of the 16-byte staging (every line starts 16-byte aligned and its row
                           // holds the n points rounded up to 4)
+  // Strided lines of the register path, half-length DCT-I, staged by TMA
+  // (tma = 1): the CTA's lines in groups of four adjacent lines (na_lines and
+  // lead make every group start 16-byte aligned), each group tma_chunks boxes
+  // of 4 x tma_box elements of the kernel's tensor map at (x, line axis,
+  // other axis) = (tma_x0 + qa', tma_m0 + chunk * tma_box, tma_b0 + qb), into
+  // shared memory as [group][point][4] (a group every 4 tma_rows floats).
+  int tma, tma_x0, tma_m0, tma_b0, tma_box, tma_chunks, tma_rows;
+  int *err;               // set to 1 if a CTA gave up waiting for its TMA loads
   double scale;           // output multiplier (inverse normalisation), 1 otherwise
   // kModeFwdEigInv only: 1/(lambda_x + lambda_y + lambda_z) on the owner block,
   // z fastest, computed in double at set-up, zero mode 0.
@@ -379,6 +388,15 @@ __device__ __forceinline__ void dct_half_input_staged(const T *la, const T *lb, 
   dct_half_pre<N1>(make_float2(la[m], lb[m]), make_float2(la[N - m], lb[N - m]), n1, sct, v, x1);
 }
 
+// The same from the TMA staging of strided lines: point m of the pair at
+// g[4 m] (the pair's two lines adjacent in a group of four).
+template <typename T, int N1>
+__device__ __forceinline__ void dct_half_input_tma(const T *g, int m, int n1, int N, typename Vec2<T>::type sct,
+                                                   typename Vec2<T>::type &v, typename Vec2<T>::type &x1) {
+  dct_half_pre<N1>(*reinterpret_cast<const float2 *>(g + 4 * m), *reinterpret_cast<const float2 *>(g + 4 * (N - m)),
+                   n1, sct, v, x1);
+}
+
 // Z of the pair in registers (x[r*N2 + k2] = Z_k, k = t + N2 (r + R k2),
 // from reg_fft_core without STORE) -> row[m] = X_m (m <= N) of both lines.
 // Thread t takes k = c N2 + t for c < C = N1/2 (k < N/2); the mirror Z_{N-k}
@@ -548,7 +566,8 @@ struct RegMinBlocks {
 };
 
 template <typename T, int N1, int N2, int MODE, int KIND>
-__global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kernel_reg(LineArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v)
+    line_kernel_reg(LineArgs<T> a, const __grid_constant__ CUtensorMap tmap) {
   static_assert(sizeof(T) == 4, "the register path stages 4-byte elements");
   static_assert(KIND == 1 || KIND == 2, "real DFT or half-length DCT-I");
   using T2 = typename Vec2<T>::type;
@@ -556,7 +575,14 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   constexpr int ROW = RegShape<N1, N2>::ROW;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ LineTable table;
+  __shared__ uint64_t tbar;
   T2 *s = reinterpret_cast<T2 *>(smem_raw);
+  // the TMA staging starts 128-byte aligned inside the rows (their bytes
+  // exceed the staging's by more than 128)
+  T *const stg = reinterpret_cast<T *>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
+  // (not in the fused z sweep: its second pass reads the rows, and the two
+  // input paths in one pass loop raised its spills)
+  const bool tma = KIND == 2 && MODE != kModeFwdEigInv && a.tma;
   const long total = (long)a.na_lines * a.nb;
   const long line0 = (long)blockIdx.x * 2 * a.P;
   const int pp = threadIdx.x / N2, t = threadIdx.x % N2;
@@ -564,13 +590,29 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
   const int n = a.n;
   const int nl = 2 * a.P;
 
-  fill_line_table(table, a, line0, total);
+  if (tma && threadIdx.x == 0) {
+    mbar_init(&tbar, 1);
+    mbar_init_fence();
+  }
+  fill_line_table(table, a, line0, total);  // (ends with a CTA barrier)
   // One 128-byte global segment per warp access: strided lines put 32
   // consecutive lines (consecutive addresses) on the lanes of a warp at one m,
   // x lines put a warp on one line. (Splitting a warp into two 16-line or
   // two-line halves makes the 4-byte shared-memory writes conflict free but
   // halves the segments, and ran slower.)
-  if (a.line_fast && a.pair8) {
+  if (tma) {
+    // thread 0 loads the P / 2 groups of four lines; every thread waits
+    if (threadIdx.x == 0) {
+      const int ng = a.P / 2;
+      mbar_expect_tx(&tbar, (unsigned)(ng * a.tma_rows * 4 * sizeof(T)));
+      for (int q = 0; q < ng; ++q) {
+        const long g0 = line0 + 4 * q;
+        const int x = a.tma_x0 + (int)(g0 % a.na_lines), b = a.tma_b0 + (int)(g0 / a.na_lines);
+        for (int c = 0; c < a.tma_chunks; ++c)
+          tma_load_3d(stg + (q * a.tma_rows + c * a.tma_box) * 4, &tmap, x, a.tma_m0 + c * a.tma_box, b, &tbar);
+      }
+    }
+  } else if (a.line_fast && a.pair8) {
     // pair p of the CTA is lines 2p, 2p+1, adjacent in memory from an even
     // address: one 8-byte copy per point (16 pairs of a warp span 128 bytes)
     const int p = threadIdx.x & (a.P - 1), ms = blockDim.x >> (a.lg_lines - 1);
@@ -637,10 +679,15 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
       for (const char *q = e0 + 128 * threadIdx.x; q < e1; q += 128 * kThreads)
         asm volatile("prefetch.global.L2 [%0];\n" ::"l"(q));
   }
-  cp_async_wait_all();
-  __syncthreads();
+  if (tma) {
+    // a wait that gives up is recorded; the CTA still runs to its end
+    if (!mbar_wait(&tbar, 0) && a.err) atomicExch(a.err, 1);
+  } else {
+    cp_async_wait_all();
+    __syncthreads();
+  }
   const T2 *src = row;
-  // (the fused z sweep's lines are always strided: no staging code there)
+  // (the fused z sweep's lines are always strided: no x-line staging there)
   const bool staged = KIND == 2 && MODE != kModeFwdEigInv && !a.line_fast && a.vec16;
   const T *ea = nullptr, *eb = nullptr;
   if (MODE == kModeFwdEigInv) ea = a.eig + table.eoff[2 * pp] * n, eb = a.eig + table.eoff[2 * pp + 1] * n;
@@ -660,24 +707,34 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v) line_kern
     T2 x1 = {T(0), T(0)};  // kind 2: the pair's partial X_1
     T2 sct = {T(0), T(1)};
     if (KIND == 2) sct = __ldg(a.dsc + t);
+    // the first FFT's inputs, one unrolled loop per input layout (the layout
+    // is uniform across the CTA, chosen once)
+    auto gather = [&](auto input) {
 #pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1) {
-      const int m = n1 * N2 + t;
-      T2 v;
-      if (KIND == 2 && staged && pass == 0) {
-        const T *lab = reinterpret_cast<const T *>(smem_raw) + (long)2 * pp * a.vec16;
-        dct_half_input_staged<T, N1>(lab, lab + a.vec16, m, n1, L, sct, v, x1);
-      } else if (KIND == 2) {
-        dct_half_input<T, N1>(row, m, n1, L, sct, v, x1);
-      } else {
-        v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, L, MODE == kModeInverse)
-                      : row[m];
+      for (int n1 = 0; n1 < N1; ++n1) {
+        T2 v;
+        input(n1 * N2 + t, n1, v);
+        if (plus) v.y = -v.y;
+        x[n1] = v;
       }
-      if (plus) v.y = -v.y;
-      x[n1] = v;
+    };
+    if constexpr (KIND == 2) {
+      if (tma && pass == 0) {
+        const T *g = stg + (pp >> 1) * a.tma_rows * 4 + (pp & 1) * 2;
+        gather([&](int m, int n1, T2 &v) { dct_half_input_tma<T, N1>(g, m, n1, L, sct, v, x1); });
+      } else if (staged && pass == 0) {
+        const T *lab = reinterpret_cast<const T *>(smem_raw) + (long)2 * pp * a.vec16;
+        gather([&](int m, int n1, T2 &v) { dct_half_input_staged<T, N1>(lab, lab + a.vec16, m, n1, L, sct, v, x1); });
+      } else {
+        gather([&](int m, int n1, T2 &v) { dct_half_input<T, N1>(row, m, n1, L, sct, v, x1); });
+      }
+    } else {
+      gather([&](int m, int, T2 &v) {
+        v = pass == 0 ? reg_input<T2>([&](int q) { return src[q]; }, m, L, MODE == kModeInverse) : row[m];
+      });
     }
     if constexpr (KIND == 2) {
-      reg_fft_core<T, N1, N2, false>(x, row, t, a.tw, false, staged && pass == 0);
+      reg_fft_core<T, N1, N2, false>(x, row, t, a.tw, false, (staged || tma) && pass == 0);
       const bool scale_eig = MODE == kModeFwdEigInv && pass == 0;
       dct_half_output<T, N1, N2>(x, row, t, x1, scale_eig ? ea : nullptr, scale_eig ? eb : nullptr);
     } else {
@@ -788,9 +845,11 @@ struct RegKernels {
 };
 
 template <typename T>
-static void launch_reg(int n1, int n2, int mode, unsigned grid, size_t smem, cudaStream_t stream, LineArgs<T> a) {
+static void launch_reg(int n1, int n2, int mode, unsigned grid, size_t smem, cudaStream_t stream, LineArgs<T> a,
+                       const CUtensorMap &tmap) {
   const void *fn = RegKernels<T>::get(n1, n2, mode, a.kind);
-  void *args[] = {&a};
+  CUtensorMap map = tmap;
+  void *args[] = {&a, &map};
   cudaLaunchKernel(fn, dim3(grid), dim3(kThreads), args, smem, stream);
 }
 
@@ -1041,7 +1100,6 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
       a.na_lines = (a.na + a.lead + 1) / 2 * 2;
       a.pair8 = 1;
     }
-    const long total = (long)a.na_lines * a.nb;
     if (ax.reg_n1) {
       a.P = ax.reg_P;
       a.lg_lines = ax.reg_lg;
@@ -1050,6 +1108,32 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
       a.dsc = ax.dsc;
       if (ax.reg_half) a.kind = 2;
       a.vec16 = 0;
+      CUtensorMap tmap{};
+      if (std::is_same<T, float>::value && a.kind == 2 && a.pair8 && d != 0 && a.P % 2 == 0 && mode != kModeFwdEigInv) {
+        // TMA staging of the strided y / z lines in groups of four: the
+        // line axis in tma_chunks boxes of at most 256 points (a multiple of
+        // 8, so every box lands 128-byte aligned), groups from a 16-byte
+        // aligned x (lead: the owner origin's offset from it)
+        const int chunks = (a.n + 255) / 256;
+        const int box = ((a.n + chunks - 1) / chunks + 7) / 8 * 8;
+        const int rows = chunks * box, lead = g.own_lo[0] % 4;
+        const bool fits = (long)(a.P / 2) * rows * 4 * (long)sizeof(T) + 128 <= (long)ax.reg_smem;
+        const long dims[3] = {g.PX, d == 1 ? g.PY : g.PZ, d == 1 ? g.PZ : g.PY};
+        const long strides[2] = {(d == 1 ? g.sy() : g.sz()) * (long)sizeof(T),
+                                 (d == 1 ? g.sz() : g.sy()) * (long)sizeof(T)};
+        if (fits && box <= 256 && make_map_3d(&tmap, phi, (int)sizeof(T), dims, strides, 4, box)) {
+          a.tma = 1;
+          a.lead = lead;
+          a.na_lines = (a.na + lead + 3) / 4 * 4;
+          a.tma_x0 = g.own_lo[0] - lead;
+          a.tma_m0 = g.own_lo[d];
+          a.tma_b0 = g.own_lo[d == 1 ? 2 : 1];
+          a.tma_box = box;
+          a.tma_chunks = chunks;
+          a.tma_rows = rows;
+          a.err = err_flag;
+        }
+      }
       if (d == 0 && a.kind == 2) {
         // 16-byte staging of the x lines: every line start 16-byte aligned
         // (the strides are multiples of 8 elements), the rounded-up line
@@ -1063,11 +1147,13 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
         const bool in_row = (long)g.own_lo[0] + (a.n + 3) / 4 * 4 <= g.PX;
         if (aligned && in_row && nl * pitch * (long)sizeof(T) <= (long)ax.reg_smem) a.vec16 = (int)pitch;
       }
+      const long total = (long)a.na_lines * a.nb;
       const unsigned grid = (unsigned)((total + 2 * a.P - 1) / (2 * a.P));
-      launch_reg<T>(ax.reg_n1, ax.reg_n2, mode, grid, ax.reg_smem, stream, a);
+      launch_reg<T>(ax.reg_n1, ax.reg_n2, mode, grid, ax.reg_smem, stream, a, tmap);
       if (launches) ++*launches;
       return;
     }
+    const long total = (long)a.na_lines * a.nb;
     const unsigned grid = (unsigned)((total + 2 * ax.P - 1) / (2 * ax.P));
     if (mode == kModeForward)
       line_kernel<T, kModeForward><<<grid, kThreads, ax.smem, stream>>>(a);

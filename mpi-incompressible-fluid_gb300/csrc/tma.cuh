@@ -73,5 +73,8 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
 // of `elem` bytes, 4 float or 8 double), box bx x by x 1, zero fill outside.
 // Returns false if the driver rejects it.
 bool make_field_map(CUtensorMap *map, const void *base, int elem, long PX, long PY, long PZ, int bx, int by);
+// The same over any 3-D view: dims[3] elements, byte strides of dims 1 and 2.
+bool make_map_3d(CUtensorMap *map, const void *base, int elem, const long dims[3], const long strides[2], int bx,
+                 int by);
 
 }  // namespace mifgpu
