@@ -580,9 +580,7 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v)
   // the TMA staging starts 128-byte aligned inside the rows (their bytes
   // exceed the staging's by more than 128)
   T *const stg = reinterpret_cast<T *>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
-  // (not in the fused z sweep: its second pass reads the rows, and the two
-  // input paths in one pass loop raised its spills)
-  const bool tma = KIND == 2 && MODE != kModeFwdEigInv && a.tma;
+  const bool tma = KIND == 2 && a.tma;
   const long total = (long)a.na_lines * a.nb;
   const long line0 = (long)blockIdx.x * 2 * a.P;
   const int pp = threadIdx.x / N2, t = threadIdx.x % N2;
@@ -1109,7 +1107,7 @@ int PoissonSolver<T>::solve(T *phi, cudaStream_t stream, long long *launches, co
       if (ax.reg_half) a.kind = 2;
       a.vec16 = 0;
       CUtensorMap tmap{};
-      if (std::is_same<T, float>::value && a.kind == 2 && a.pair8 && d != 0 && a.P % 2 == 0 && mode != kModeFwdEigInv) {
+      if (std::is_same<T, float>::value && a.kind == 2 && a.pair8 && d != 0 && a.P % 2 == 0) {
         // TMA staging of the strided y / z lines in groups of four: the
         // line axis in tma_chunks boxes of at most 256 points (a multiple of
         // 8, so every box lands 128-byte aligned), groups from a 16-byte
