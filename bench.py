@@ -136,14 +136,14 @@ def step_sweeps(precision: str) -> float:
 # DRAM read + write bytes over algorithmic bytes, from ncu captures of the
 # stage, divergence and projection kernels on the 256x256x512 profiling case
 # (the compensated stages, two of them with the projection inside, on its
-# Ethier-Steinman variant: 1.08, 1.08, 1.09) and of the line sweeps on the
-# 512x256x256 one: applied to the full launch.
+# Ethier-Steinman variant: 1.05, 1.03, 1.03) and of the line sweeps on the
+# 256x512x256 one: applied to the full launch.
 # (The fused z sweep's figure includes its 1/lambda table, one more
 # field-sized read.)
 MEASURED_TRAFFIC_RATIO = {
     "mixed": {"stage": 1.06, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
               "x_inverse": 0.82},
-    "compensated": {"stage": 1.08, "divergence": 1.03, "project": 0.99, "x_forward": 0.82, "y_forward": 0.81,
+    "compensated": {"stage": 1.04, "divergence": 1.03, "project": 0.99, "x_forward": 0.82, "y_forward": 0.81,
                     "z_fused": 1.37, "y_inverse": 0.81, "x_inverse": 0.82},
 }
 # FP64 operations of one FP64 step per cell (an FMA counted as two), from the
