@@ -322,6 +322,10 @@ def test_poisson_solution_satisfies_discrete_laplacian(mifgpu_lib, cuda_device):
     ((5, 9, 385), (False, False, False)),     # register 384 = 48 x 8, z fused
     ((9, 769, 5), (False, True, False)),      # real DFT 768 along the strided y axis
     ((9, 5, 385), (False, False, True)),      # real DFT 384, z fused
+    # strided DCT-I lines staged by TMA in groups of four lines from an odd x
+    # origin (periodic x: lead 1), 513 points in three boxes
+    ((32, 513, 9), (True, False, False)),     # y sweeps
+    ((9, 17, 513), (True, False, False)),     # the fused z sweep
 ])
 def test_mixed_poisson_matches_oracle(oracle_lib, mifgpu_lib, cuda_device, shape, periodic):
     """Mixed-precision Poisson solve (register FFT for power-of-two lengths)
