@@ -57,10 +57,13 @@ enum mifgpu_precision {
                        set 0 and the error norms see hi + residual. The
                        velocity-only step and the reverse mode return
                        MIFGPU_ENOTSUP in this mode. Inside a step the Y3 and U*
-                       stage kernels apply the projection before them, so after
-                       a step velocity_buffer and velocity_buffer_2 (scratch in
-                       the reference too) hold the unprojected stage states;
-                       the context holds one more pressure-sized buffer. */
+                       stage kernels apply the projection before them, and in
+                       a run of several steps each step's Y2 stage applies the
+                       previous step's last projection (the run's last step
+                       ends with it), so after a call velocity_buffer and
+                       velocity_buffer_2 (scratch in the reference too) hold
+                       unprojected stage states; the context holds two more
+                       pressure-sized buffers. */
 };
 
 /* Analytic field families used for Dirichlet boundary data, forcing and

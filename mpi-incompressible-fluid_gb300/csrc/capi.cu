@@ -207,6 +207,10 @@ struct Impl final : ImplBase {
   // projection themselves (StageProj: the Y3 stage writes p + phi here, the
   // U* stage reads it and writes the pressure field).
   T *p_alt = nullptr;
+  // ... and a third one: within a run of several steps the Y2 stage applies
+  // the previous step's last projection too, and the pressure cycles
+  // p -> p_alt (Y2) -> p_alt2 (Y3) -> p (U*).
+  T *p_alt2 = nullptr;
   double *face_tab = nullptr;  // float path: the families' face data in double; or the caller's
   FaceTables ftabs{};
   // Caller pressure-gradient face data (slots 0..3), allocated on first use.
@@ -214,8 +218,9 @@ struct Impl final : ImplBase {
   GradFaces gfaces{};
   std::vector<double> pack;  // host packing buffer of the caller data
   cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t graph[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
-  long long graph_launches[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+  // Step graphs per variant, labelling parity and phase (kPhase*).
+  cudaGraphExec_t graph[3][2][4] = {};
+  long long graph_launches[3][2][4] = {};
   size_t total_bytes = 0;
   // Per-kernel-class event marks of a profiled (non-graph) step.
   std::vector<std::pair<int, cudaEvent_t>> *prof = nullptr;
@@ -247,8 +252,9 @@ struct Impl final : ImplBase {
 
   ~Impl() override {
     for (auto &gv : graph)
-      for (auto &gx : gv)
-        if (gx) cudaGraphExecDestroy(gx);
+      for (auto &gp : gv)
+        for (auto &gx : gp)
+          if (gx) cudaGraphExecDestroy(gx);
     ps.release();
     cudaFree(block);
     cudaFree(ftab);
@@ -260,6 +266,7 @@ struct Impl final : ImplBase {
     cudaFree(grad_block);
     cudaFree(res_block);
     cudaFree(p_alt);
+    cudaFree(p_alt2);
     cudaFree(face_tab);
     cudaFree(grad_tab);
     cudaFree(adj_block);
@@ -297,10 +304,12 @@ struct Impl final : ImplBase {
       total_bytes += sizeof(__nv_bfloat16) * field_elems * 3;
       CK(cudaMemset(res_block, 0, sizeof(__nv_bfloat16) * field_elems * 3));
       for (int c = 0; c < 3; ++c) res.c[c] = res_block + c * field_elems;
-      if (cudaMalloc(&p_alt, sizeof(T) * field_elems) != cudaSuccess)
-        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the second pressure buffer failed");
-      total_bytes += sizeof(T) * field_elems;
+      if (cudaMalloc(&p_alt, sizeof(T) * field_elems) != cudaSuccess ||
+          cudaMalloc(&p_alt2, sizeof(T) * field_elems) != cudaSuccess)
+        return fail(ctx, MIFGPU_ENOMEM, "cudaMalloc of the extra pressure buffers failed");
+      total_bytes += 2 * sizeof(T) * field_elems;
       CK(cudaMemset(p_alt, 0, sizeof(T) * field_elems));
+      CK(cudaMemset(p_alt2, 0, sizeof(T) * field_elems));
     }
     std::string perr;
     const int rc = ps.init(g, perr);
@@ -629,7 +638,16 @@ struct Impl final : ImplBase {
 
   // The kernels of one step of the given variant, in stream order. False
   // if a stage kernel could not be launched (its tensor maps were rejected).
-  bool enqueue_step(mifgpu_ctx *ctx, cudaStream_t s, int variant, long long *cnt) {
+  //
+  // Phases (compensated projection steps; every other step is kPhaseFull):
+  // in a run of several steps the step's last projection is left to the next
+  // step's Y2 stage, which applies it to its ring as the Y3 and U* stages do
+  // theirs. The run's first step has no projection to take over (first), the
+  // later ones do (rest); the last step of the run ends with the projection
+  // kernel (closed), the others do not (open). Sets and pressure after an
+  // open step: set 0 and p lack the step's last projection, phi holds it.
+  enum { kPhaseFull = 0, kPhaseFirstOpen = 1, kPhaseRestOpen = 2, kPhaseRestClosed = 3 };
+  bool enqueue_step(mifgpu_ctx *ctx, cudaStream_t s, int variant, long long *cnt, int phase = kPhaseFull) {
     const double dt = g.dt;
     ForcingTables<T> ft{ftab, ftab_maxE};
     const int kind = ctx->prm.boundary_kind;
@@ -656,36 +674,44 @@ struct Impl final : ImplBase {
     // In the compensated state the Y3 and U* stage kernels apply the
     // projection before them (StageProj): the projected sets 1 and 2 are read
     // by those stages only, so they are never stored. The pressure goes
-    // p -> p_alt (Y3) -> p (U*), and the last projection is a kernel of its own.
+    // p -> p_alt (Y3) -> p (U*), and the last projection is a kernel of its own
+    // (or, in the rest phases, p -> p_alt (Y2) -> p_alt2 (Y3) -> p (U*)).
     const bool fused = res.on() && p_alt;
+    const bool rest = fused && (phase == kPhaseRestOpen || phase == kPhaseRestClosed);
+    const bool closed = !fused || phase == kPhaseFull || phase == kPhaseRestClosed;
+    T *const pbuf[4] = {F.f[kP], p_alt, rest ? p_alt2 : F.f[kP], F.f[kP]};  // p before stage st, after U*
     for (int st = 0; st < 3; ++st) {
       StageScalars<T> sc{dt, sin_slot[st], ctx->prm.forcing, ctx->prm.forcing_amplitude};
       StageProj pj{};
+      const bool proj = fused && (st > 0 || rest);
       if constexpr (std::is_same<T, float>::value) {
+        // stage st applies the projection of stage st - 1 (the previous
+        // step's U* for the Y2 stage)
+        const int prev = st == 0 ? 2 : st - 1;
         pj.phi = F.f[kPhi];
-        pj.p_in = st == 1 ? F.f[kP] : p_alt;
-        pj.p_out = st == 1 ? p_alt : F.f[kP];
-        pj.dt = float(dts[st - 1 < 0 ? 0 : st - 1]);
-        pj.tag = 16u + (st - 1 < 0 ? 0 : st - 1);
+        pj.p_in = rest ? pbuf[st] : (st == 1 ? F.f[kP] : p_alt);
+        pj.p_out = rest ? pbuf[st + 1] : (st == 1 ? p_alt : F.f[kP]);
+        pj.dt = float(dts[prev]);
+        pj.tag = 16u + prev;
       }
       // in the compensated state every stage's output set carries the residuals
       mark(MIFGPU_PROF_STAGE, s);
-      ok &= launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res, fused && st > 0 ? &pj : nullptr,
-                            kerr);
+      ok &= launch_stage<T>(g, F, kinds[st], sc, ft, kind, tref(), s, cnt, res, proj ? &pj : nullptr, kerr);
       enqueue_bc(ctx, s, out_set[st], 1 + st, cnt, res);
       enqueue_pressure(ctx, s, out_set[st], dts[st], nhn, 1 + st, st, true, cnt, res);
       // the last projection of the step watches phi for NaN / Inf
-      if (!fused || st == 2) enqueue_project(s, out_set[st], dts[st], 16u + st, cnt, res, st == 2 ? nonfinite : nullptr);
+      if (!fused || (st == 2 && closed))
+        enqueue_project(s, out_set[st], dts[st], 16u + st, cnt, res, st == 2 ? nonfinite : nullptr);
     }
     return ok;
   }
 
-  int ensure_graph(mifgpu_ctx *ctx, int variant) {
-    if (graph[variant][parity]) return MIFGPU_OK;
+  int ensure_graph(mifgpu_ctx *ctx, int variant, int phase = kPhaseFull) {
+    if (graph[variant][parity][phase]) return MIFGPU_OK;
     cudaGraph_t gr = nullptr;
     CK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
     long long cnt = 0;
-    const bool launched = enqueue_step(ctx, cap_stream, variant, &cnt);
+    const bool launched = enqueue_step(ctx, cap_stream, variant, &cnt, phase);
     advance_step_kernel<<<1, 1, 0, cap_stream>>>(step_ctr);
     ++cnt;
     cudaError_t e = cudaStreamEndCapture(cap_stream, &gr);
@@ -694,10 +720,10 @@ struct Impl final : ImplBase {
       cudaGraphDestroy(gr);
       return fail(ctx, MIFGPU_ECUDA, "cuTensorMapEncodeTiled rejected a stage kernel's tile map");
     }
-    e = cudaGraphInstantiate(&graph[variant][parity], gr, 0);
+    e = cudaGraphInstantiate(&graph[variant][parity][phase], gr, 0);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
-    graph_launches[variant][parity] = cnt;
+    graph_launches[variant][parity][phase] = cnt;
     return MIFGPU_OK;
   }
 
@@ -706,7 +732,18 @@ struct Impl final : ImplBase {
   // relabelling: its replays alternate the graphs of the two labellings.
   int step(mifgpu_ctx *ctx, int variant, const double *host_slots, int nsteps) override {
     const bool swap = variant == kVariantVelocity;
-    if (int rc = ensure_graph(ctx, variant)) return rc;
+    // the compensated projection steps of a run of several steps hand each
+    // step's last projection to the next step (enqueue_step's phases)
+    const bool chain = res.on() && p_alt && !swap && nsteps > 1;
+    auto phase_of = [&](int n) {
+      return !chain ? kPhaseFull : n == 0 ? kPhaseFirstOpen : n == nsteps - 1 ? kPhaseRestClosed : kPhaseRestOpen;
+    };
+    if (chain) {
+      for (int ph : {kPhaseFirstOpen, kPhaseRestOpen, kPhaseRestClosed})
+        if (int rc = ensure_graph(ctx, variant, ph)) return rc;
+    } else if (int rc = ensure_graph(ctx, variant)) {
+      return rc;
+    }
     if (swap && nsteps > 1) {
       swap_sets();
       const int rc = ensure_graph(ctx, variant);
@@ -720,8 +757,9 @@ struct Impl final : ImplBase {
                          cudaMemcpyHostToDevice, ctx->stream));
       CK(cudaMemsetAsync(step_ctr, 0, sizeof(int), ctx->stream));
       for (int n = 0; n < chunk; ++n) {
-        CK(cudaGraphLaunch(graph[variant][parity], ctx->stream));
-        ctx->launches += graph_launches[variant][parity];
+        const int ph = phase_of(n0 + n);
+        CK(cudaGraphLaunch(graph[variant][parity][ph], ctx->stream));
+        ctx->launches += graph_launches[variant][parity][ph];
         if (swap) swap_sets();
       }
     }
@@ -989,8 +1027,8 @@ struct Impl final : ImplBase {
       for (int m = 0; m < len && e == cudaSuccess; ++m) {
         T *snap = b >= 0 ? sn(b * C + m) : nullptr;
         if (snap) e = copy_fields(snap, set0, 3, st);
-        if (e == cudaSuccess) e = cudaGraphLaunch(graph[kVariantProjection][parity], st);
-        *cnt += graph_launches[kVariantProjection][parity];
+        if (e == cudaSuccess) e = cudaGraphLaunch(graph[kVariantProjection][parity][kPhaseFull], st);
+        *cnt += graph_launches[kVariantProjection][parity][kPhaseFull];
         if (snap && e == cudaSuccess) e = copy_fields(snap + 3 * field_elems, set1, 3, st);
         if (snap && e == cudaSuccess) e = copy_fields(snap + 6 * field_elems, set2, 3, st);
       }
@@ -1131,11 +1169,12 @@ struct Impl final : ImplBase {
   void drop_graphs() override {
     drop_rev_graphs();
     for (auto &gv : graph)
-      for (auto &gx : gv)
-        if (gx) {
-          cudaGraphExecDestroy(gx);
-          gx = nullptr;
-        }
+      for (auto &gp : gv)
+        for (auto &gx : gp)
+          if (gx) {
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
+          }
   }
 
   size_t bytes() const override { return total_bytes; }

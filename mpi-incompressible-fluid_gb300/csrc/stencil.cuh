@@ -80,8 +80,8 @@ struct StageScalars {
   double alpha;  // amplitude of the Taylor-Green body force
 };
 
-// The projection that precedes a compensated Y3 or U* stage, applied by the
-// stage kernel itself (see stage_proj_kernel): phi of the previous solve, the
+// The projection that precedes a compensated stage, applied by the stage
+// kernel itself (see stage_proj_kernel): phi of the previous solve, the
 // pressure read (p_in) and written as p + phi (p_out, another buffer), and the
 // previous projection's dt and stochastic-rounding tag (launch_project's).
 struct StageProj {
@@ -93,7 +93,7 @@ struct StageProj {
 };
 
 // `res`: the compensated state's residuals (projection stages, float only).
-// `proj` (compensated kStageY3 / kStageUStar only, or null): the preceding
+// `proj` (compensated projection stages only, or null): the preceding
 // projection, done inside the stage. The plane ring is filled by TMA tile
 // loads; `kerr` (device, may be null) is set to 1 if a CTA gave up waiting
 // for one. Returns false (nothing launched) if a tensor map was rejected.

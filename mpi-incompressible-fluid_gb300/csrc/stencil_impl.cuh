@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
   (void)sz;
 }
 
-// ---- compensated Y3 / U* stage with the previous projection inside ----
+// ---- compensated stage with the previous projection inside ----
 //
 // In the compensated state the projections that follow the Y2 and Y3 stages
 // (src/Timestep.cpp:97-141) are applied by the next stage kernel to its own
@@ -481,7 +481,8 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
 // stage only, so the projected velocity never goes back to memory: per step
 // this saves two projection passes (the velocity and residual read and
 // written, twelve float sweeps each) for one more ring field (phi) and the
-// pressure update, written here.
+// pressure update, written here. Between the steps of one run the step's
+// last projection is applied the same way by the next step's Y2 stage.
 //
 // Ring values: u' = fl(u + inc), inc = -(((phi - phi_b) * oh) * dt) with
 // phi_b the neighbour one step back along the component's axis, on the
@@ -527,7 +528,10 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
     stage_proj_kernel(Geometry g, Coeffs<float> co, Fields<float> F, StageCoef<float> K, ForcingEval<float> fe,
                       TimeRef tr, int sin_slot, int kc, Residual res, StageProj pj,
                       const __grid_constant__ StageMaps maps, int *kerr) {
-  static_assert(ST == kStageY3 || ST == kStageUStar, "the stages that follow a projection");
+  static_assert(ST == kStageY2 || ST == kStageY3 || ST == kStageUStar, "the projection stages");
+  // the other set read at the own point: set 2 (Y2's right-hand side) for Y3,
+  // set 0 (Y3's scaled one) for U*; Y2 reads none
+  constexpr bool kOth = ST != kStageY2;
   constexpr int oth_set = ST == kStageY3 ? 2 : 0;
   __shared__ __align__(128) RingProj ring;
   __shared__ uint64_t bars[4];
@@ -594,9 +598,11 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   auto prefetch = [&](int kk) {
     if (!in_box || kk >= kend) return;
     const long po = (long)kk * plane;
-    n0 = oth0[po];
-    n1 = oth1[po];
-    n2 = oth2[po];
+    if (kOth) {
+      n0 = oth0[po];
+      n1 = oth1[po];
+      n2 = oth2[po];
+    }
     l0 = res0[po];
     l1 = res1[po];
     l2 = res2[po];
@@ -736,7 +742,11 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
       const float self = tp.self(c);
       const float cur = c == 0 ? c0 : (c == 1 ? c1 : c2), lo = c == 0 ? lo0 : (c == 1 ? lo1 : lo2);
       __nv_bfloat16 *lo_out = res.c[c] + q;
-      if constexpr (ST == kStageY3) {
+      if constexpr (ST == kStageY2) {
+        F.vel(1, c)[q] = comp_add(self, lo, K.k1 * r - K.k3 * gp, lo_out);
+        F.vel(2, c)[q] = r;
+        (void)cur;
+      } else if constexpr (ST == kStageY3) {
         const float r2s = K.k2 * r;
         F.vel(2, c)[q] = comp_add(self, lo, K.k1 * cur + r2s - K.k3 * gp, lo_out);
         F.vel(0, c)[q] = r2s;
@@ -1446,7 +1456,7 @@ struct StageLaunch {
                            : (ST == kStageY3 || ST == kVelY3)                  ? 1
                                                                                : 2;
     StageMaps m;
-    if constexpr (std::is_same<T, float>::value && (ST == kStageY3 || ST == kStageUStar)) {
+    if constexpr (std::is_same<T, float>::value && ST <= kStageUStar) {
       if (comp && proj) {
         if (!maps_for(in_set, true, m)) return false;
         if (forcing)
