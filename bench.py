@@ -123,14 +123,20 @@ def launches_per_step(precision: str) -> dict:
     return out
 
 
-def step_sweeps(precision: str) -> float:
+def step_sweeps(precision: str, steps: int = 1) -> float:
     """Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps +
     9 projection) = 102 in FP64 and the plain float mode. The compensated
-    state: stages 13 + 18 + 15 (residuals, and phi and p + phi in the two
-    stages that project), 3 x 5.5 divergence, 30 line sweeps and one
-    projection of 12: 104.5."""
+    state, one step: stages 13 + 18 + 15 (residuals, and phi and p + phi in
+    the two stages that project), 3 x 5.5 divergence, 30 line sweeps and one
+    projection of 12: 104.5. In a run of `steps` steps each later step's Y2
+    stage also projects (15 instead of 13) and the projection kernel runs
+    once, at the end: the mean per step is 104.5 - 12 + (2 (steps - 1) + 12) /
+    steps (95.0 for 20 steps)."""
     n = launches_per_step(precision)
-    return sum(v * n[k] for k, v in sweeps(precision).items())
+    one = sum(v * n[k] for k, v in sweeps(precision).items())
+    if precision == "compensated" and steps > 1:
+        return one - 12.0 + (2.0 * (steps - 1) + 12.0) / steps
+    return one
 
 
 # DRAM read + write bytes over algorithmic bytes, from ncu captures of the
@@ -889,7 +895,7 @@ def run_gpu(args):
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": round(avg_launch_ms, 4)}
     step_ms = ms / args.steps
-    ssw = step_sweeps(prec)
+    ssw = step_sweeps(prec, args.steps)
     step_roofline = ssw * elem * cells / (step_ms / 1e3) / 1e9
     per_kernel = {k: {"ms_per_step": round(v, 4),
                       "gbs": round(sw[k] * nl[k] * elem * cells / (v / 1e3) / 1e9, 1),
