@@ -109,47 +109,47 @@ def sweeps(precision: str) -> dict:
     if precision == "compensated":
         for k, v in COMPENSATED_EXTRA.items():
             out[k] += v
-        # The Y3 and U* stage kernels apply the projection before them
-        # (stage_proj_kernel): each also reads phi and writes p + phi.
-        out["stage"] += 4.0 / 3.0
+        # The stage kernels of the step a run repeats (the one profile_step
+        # times) apply the projection before them (stage_proj_kernel): each
+        # also reads phi and writes p + phi (15, 18, 15).
+        out["stage"] += 2.0
     return out
 
 
 def launches_per_step(precision: str) -> dict:
-    """In the compensated state only the step's last projection is a kernel of its own."""
+    """In the compensated state the step a run repeats has no projection kernel."""
     out = dict(LAUNCHES_PER_STEP)
     if precision == "compensated":
-        out["project"] = 1
+        out["project"] = 0
     return out
 
 
 def step_sweeps(precision: str, steps: int = 1) -> float:
     """Per step as built: 33 stage + 3 x (4 divergence + 5 x 2 line sweeps +
     9 projection) = 102 in FP64 and the plain float mode. The compensated
-    state, one step: stages 13 + 18 + 15 (residuals, and phi and p + phi in
-    the two stages that project), 3 x 5.5 divergence, 30 line sweeps and one
-    projection of 12: 104.5. In a run of `steps` steps each later step's Y2
-    stage also projects (15 instead of 13) and the projection kernel runs
-    once, at the end: the mean per step is 104.5 - 12 + (2 (steps - 1) + 12) /
-    steps (95.0 for 20 steps)."""
+    state, the step a run repeats: stages 15 + 18 + 15 (residuals, and phi and
+    p + phi in the stages that project), 3 x 5.5 divergence, 30 line sweeps:
+    94.5. A run's first step has a plain Y2 stage (13) and its last ends with
+    the projection kernel (12): over a run of `steps` steps the mean is
+    94.5 + (12 - 2) / steps (95.0 for 20 steps; 104.5 for one step)."""
     n = launches_per_step(precision)
-    one = sum(v * n[k] for k, v in sweeps(precision).items())
-    if precision == "compensated" and steps > 1:
-        return one - 12.0 + (2.0 * (steps - 1) + 12.0) / steps
-    return one
+    rep = sum(v * n[k] for k, v in sweeps(precision).items())
+    if precision == "compensated":
+        return rep + (12.0 - 2.0) / max(1, steps)
+    return rep
 
 
 # DRAM read + write bytes over algorithmic bytes, from ncu captures of the
 # stage, divergence and projection kernels on the 256x256x512 profiling case
-# (the compensated stages, two of them with the projection inside, on its
-# Ethier-Steinman variant: 1.05, 1.03, 1.03) and of the line sweeps on the
-# 256x512x256 one: applied to the full launch.
+# (the compensated stages with the projection inside, of the step a run
+# repeats, on its Ethier-Steinman variant: 1.04, 1.03, 1.03) and of the line
+# sweeps on the 256x512x256 one: applied to the full launch.
 # (The fused z sweep's figure includes its 1/lambda table, one more
 # field-sized read.)
 MEASURED_TRAFFIC_RATIO = {
     "mixed": {"stage": 1.06, "x_forward": 0.82, "y_forward": 0.81, "z_fused": 1.37, "y_inverse": 0.81,
               "x_inverse": 0.82},
-    "compensated": {"stage": 1.04, "divergence": 1.03, "project": 0.99, "x_forward": 0.82, "y_forward": 0.81,
+    "compensated": {"stage": 1.03, "divergence": 1.03, "project": 0.99, "x_forward": 0.82, "y_forward": 0.81,
                     "z_fused": 1.37, "y_inverse": 0.81, "x_inverse": 0.82},
 }
 # FP64 operations of one FP64 step per cell (an FMA counted as two), from the

@@ -284,7 +284,10 @@ enum mifgpu_prof_class {
 /* Runs `reps` projection steps from t_n launch by launch (not from the graph),
  * timing every kernel class with CUDA events on the context's stream; writes
  * the mean milliseconds per step of each class. The steps are real: the
- * fields advance. No counterpart in the reference (instrumentation). */
+ * fields advance. In MIFGPU_MIXED_COMPENSATED the timed step is the one a
+ * run of several steps repeats (its Y2 stage applies the previous step's last
+ * projection; no projection kernel of its own), with one untimed step before
+ * and one after. No counterpart in the reference (instrumentation). */
 int mifgpu_profile_step(mifgpu_ctx *ctx, double t_n, int reps, double ms_out[MIFGPU_PROF_CLASSES]);
 
 /* ---- Reverse mode (no counterpart in the reference) ----
