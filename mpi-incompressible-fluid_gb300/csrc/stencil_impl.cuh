@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
 // pressure update, written here. Between the steps of one run the step's
 // last projection is applied the same way by the next step's Y2 stage.
 //
-// Ring values: u' = fl(u + inc), inc = -(((phi - phi_b) * oh) * dt) with
+// Ring values: u' = fl(u + inc), inc = (phi_b - phi) * (oh * dt) with
 // phi_b the neighbour one step back along the component's axis, on the
 // points project_pair_kernel updates (interior of the component), the others
 // as they are. The stencils read these float values as they read the
@@ -494,8 +494,8 @@ __global__ void __launch_bounds__(kTX *kTY, sizeof(T) == 4 ? (kComp ? kStageMinB
 // the stored residual), so the update adds its increment to u' + lo' with
 // comp_add as the unfused stage does.
 //
-// The pressure p + phi is written stochastically rounded as project_pair_kernel
-// writes it (same draws), into p_out: other CTAs still read p_in as halo. The
+// The pressure p + phi is written stochastically rounded, as
+// project_pair_kernel writes it, into p_out: other CTAs still read p_in as halo. The
 // pressure gradient of the stage uses (p + phi) unrounded, as the difference of
 // p plus the difference of phi. Pressure nodes outside the threads' range
 // (x = 0, y = 0, z = 0 and the last x node of a periodic axis when it falls on
@@ -544,7 +544,9 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   const long plane = g.sz(), PX = g.PX;
   const int PZ = (int)g.PZ;
   const int lim0 = g.ext(0, 2) - 1, lim1 = g.ext(1, 2) - 1, lim2 = g.ext(2, 2) - 1;
-  const float pdt = pj.dt, oh0 = co.oh[0], oh1 = co.oh[1], oh2 = co.oh[2];
+  const float oh0 = co.oh[0], oh1 = co.oh[1], oh2 = co.oh[2];
+  // the projection increment (phi_b - phi) * oh * dt, with oh * dt formed once
+  const float cd0 = oh0 * pj.dt, cd1 = oh1 * pj.dt, cd2 = oh2 * pj.dt;
   float *const p_out = pj.p_out;
   const int tid = threadIdx.x, tx = tid % kTX, ty = tid / kTX;
   const int i0 = 1 + blockIdx.x * kTX, j0 = 1 + blockIdx.y * kTY;
@@ -644,17 +646,17 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
       const float f0 = ph[o_p];
       float lo0 = __bfloat162float(l0), lo1 = __bfloat162float(l1), lo2 = __bfloat162float(l2);
       if (m & 1u) {
-        const float inc = -(((f0 - ph[o_p - 1]) * oh0) * pdt), hi = rb[o_r], s = __fadd_rn(hi, inc);
+        const float inc = (ph[o_p - 1] - f0) * cd0, hi = rb[o_r], s = __fadd_rn(hi, inc);
         rb[o_r] = s;
         lo0 = __fadd_rn(lo0, two_sum_err(hi, inc, s));
       }
       if (m & 2u) {
-        const float inc = -(((f0 - ph[o_p - kPhiX]) * oh1) * pdt), hi = rb[4 * kSlot + o_r], s = __fadd_rn(hi, inc);
+        const float inc = (ph[o_p - kPhiX] - f0) * cd1, hi = rb[4 * kSlot + o_r], s = __fadd_rn(hi, inc);
         rb[4 * kSlot + o_r] = s;
         lo1 = __fadd_rn(lo1, two_sum_err(hi, inc, s));
       }
       if (m & 4u) {
-        const float inc = -(((f0 - phb[o_p]) * oh2) * pdt), hi = rb[8 * kSlot + o_r], s = __fadd_rn(hi, inc);
+        const float inc = (phb[o_p] - f0) * cd2, hi = rb[8 * kSlot + o_r], s = __fadd_rn(hi, inc);
         rb[8 * kSlot + o_r] = s;
         lo2 = __fadd_rn(lo2, two_sum_err(hi, inc, s));
       }
@@ -662,16 +664,16 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
     }
     if (m & 0x38u) {
       const float f0 = ph[h_p];
-      if (m & 8u) rb[h_r] = __fadd_rn(rb[h_r], -(((f0 - ph[h_p - 1]) * oh0) * pdt));
-      if (m & 16u) rb[4 * kSlot + h_r] = __fadd_rn(rb[4 * kSlot + h_r], -(((f0 - ph[h_p - kPhiX]) * oh1) * pdt));
-      if (m & 32u) rb[8 * kSlot + h_r] = __fadd_rn(rb[8 * kSlot + h_r], -(((f0 - phb[h_p]) * oh2) * pdt));
+      if (m & 8u) rb[h_r] = __fadd_rn(rb[h_r], (ph[h_p - 1] - f0) * cd0);
+      if (m & 16u) rb[4 * kSlot + h_r] = __fadd_rn(rb[4 * kSlot + h_r], (ph[h_p - kPhiX] - f0) * cd1);
+      if (m & 32u) rb[8 * kSlot + h_r] = __fadd_rn(rb[8 * kSlot + h_r], (phb[h_p] - f0) * cd2);
     }
   };
-  // p + phi, stochastically rounded with project_pair_kernel's draws
+  // p + phi, stochastically rounded (one hash round of the point and the
+  // projection's salt gives the dither)
   const unsigned psalt = sr_salt(tr, pj.tag);
   auto p_new = [&](int r, int rp, int kk, long q) {
-    const unsigned h = sr_mix((unsigned)q ^ psalt);
-    return add_sr(ring.f[3][kk & 3][r], ring.phi[kk & 3][rp], sr_draw(sr_mix(h), 0));
+    return add_sr(ring.f[3][kk & 3][r], ring.phi[kk & 3][rp], sr_draw(sr_mix((unsigned)q ^ psalt), 0));
   };
   // Pressure nodes outside the threads' range, at the CTAs on those edges.
   const int E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
