@@ -824,6 +824,44 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
   // caller data (slot_stride > 0): the slot's own table, no time factor
   const double factor = ft.tab ? (ft.slot_stride ? 1.0 : tr.get(kSlotFactor + 4 * fn + t_slot)) : 0.0;
   const double *tab = ft.tab ? ft.tab + (long)t_slot * ft.slot_stride : nullptr;
+  if constexpr (kTable) {
+    // From the tables: the six face values (three components, both sides)
+    // are all loaded before any is stored, so their loads overlap (the
+    // compiler cannot move a table load above a field store).
+    double v[3][2];
+    long q[3][2];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        q[c][s] = -1;
+        if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) continue;
+        const long fixed = s == 0 ? 0 : g.ext(c, d) - 1;
+        const long pt[3] = {d == 0 ? fixed : pa, d == 1 ? fixed : (d == 0 ? pa : pb), d == 2 ? fixed : pb};
+        bool later = false;  // an x face beats y beats z
+        if (d >= 1 && !g.periodic[0] && (pt[0] == 0 || pt[0] == g.ext(c, 0) - 1)) later = true;
+        if (d == 2 && !g.periodic[1] && (pt[1] == 0 || pt[1] == g.ext(c, 1) - 1)) later = true;
+        if (later) continue;
+        q[c][s] = g.idx(pt[0], pt[1], pt[2]);
+        v[c][s] = __ldg(tab + ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb) * factor;
+      }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      T *f = c == 0 ? c0 : (c == 1 ? c1 : c2);
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        if (q[c][s] < 0) continue;
+        if constexpr (std::is_same<T, float>::value) {
+          if (res.on()) {  // compensated state: the double face value as hi + residual
+            f[q[c][s]] = comp_split(v[c][s], res.c[c] + q[c][s]);
+            continue;
+          }
+        }
+        f[q[c][s]] = T(v[c][s]);
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     if (pa >= g.ext(c, a) || pb >= g.ext(c, b)) continue;
@@ -837,24 +875,15 @@ __global__ void bc_faces_kernel(Geometry g, T *c0, T *c1, T *c2, int kind, int f
       if (d >= 1 && !g.periodic[0] && (pt[0] == 0 || pt[0] == g.ext(c, 0) - 1)) later = true;
       if (d == 2 && !g.periodic[1] && (pt[1] == 0 || pt[1] == g.ext(c, 1) - 1)) later = true;
       if (later) continue;
+      // evaluated in the working precision (no tables)
       const long q = g.idx(pt[0], pt[1], pt[2]);
       if constexpr (std::is_same<T, float>::value) {
-        if (res.on()) {  // compensated state: the double face value as hi + residual
-          double v;
-          if constexpr (kTable)
-            v = tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor;
-          else
-            v = (double)face_value<T>(g, c, d, s, pt, kind, fn, T(t));
-          f[q] = comp_split(v, res.c[c] + q);
+        if (res.on()) {  // compensated state: the value as hi + residual
+          f[q] = comp_split((double)face_value<T>(g, c, d, s, pt, kind, fn, T(t)), res.c[c] + q);
           continue;
         }
       }
-      T val;
-      if constexpr (kTable)
-        val = T(tab[ft.off[fn][c][d][s] + pa + (long)g.ext(c, a) * pb] * factor);
-      else
-        val = T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
-      f[q] = val;
+      f[q] = T(face_value<T>(g, c, d, s, pt, kind, fn, T(t)));
     }
   }
 }
