@@ -792,6 +792,7 @@ struct Impl final : ImplBase {
       CK(cudaStreamSynchronize(ctx->stream));
       return MIFGPU_OK;
     };
+    CK(cudaMemsetAsync(nonfinite, 0, 2 * sizeof(int), ctx->stream));
     if (chain)
       if (int rc = untimed(kPhaseFirstOpen)) return rc;
     for (int r = 0; r < reps; ++r) {
@@ -817,6 +818,9 @@ struct Impl final : ImplBase {
     }
     if (chain)
       if (int rc = untimed(kPhaseRestClosed)) return rc;
+    int flags[2] = {0, 0};
+    CK(cudaMemcpy(flags, nonfinite, sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags[1]) return fail(ctx, MIFGPU_ECUDA, "a stage or line kernel gave up waiting for a TMA tile load");
     return MIFGPU_OK;
   }
 
@@ -1012,6 +1016,7 @@ struct Impl final : ImplBase {
     }
     if (int rc = ensure_graph(ctx, kVariantProjection)) return rc;
     cudaStream_t s = ctx->stream, r = rec_stream;
+    CK(cudaMemsetAsync(nonfinite, 0, 2 * sizeof(int), s));
     long long *cnt = &ctx->launches;
     std::vector<double> sl((size_t)kSlotSize * N);
     for (int n = 0; n < N; ++n)
@@ -1134,10 +1139,13 @@ struct Impl final : ImplBase {
     CK(copy_fields(set0, ck(nseg), 3, s));
     CK(copy_fields(p, ck(nseg) + 3 * field_elems, 1, s));
     double h[2];
+    int flags[2] = {0, 0};
     CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(flags, nonfinite, sizeof(flags), cudaMemcpyDeviceToHost, s));
     cudaError_t e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "gradient");
+    if (flags[1]) return cleanup(), fail(ctx, MIFGPU_ECUDA, "a stage or line kernel gave up waiting for a TMA tile load");
     if (req.loss) *req.loss = h[0];
     if (req.dalpha) *req.dalpha = h[1];
     if (req.ms) {

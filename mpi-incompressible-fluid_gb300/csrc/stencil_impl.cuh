@@ -277,7 +277,8 @@ __device__ __forceinline__ T rhs_taps(int c, const Taps<T> &a, const Coeffs<T> &
 }
 
 // Float: 48 warps per SM at 40 registers, with a few dozen bytes of spills;
-// the march is latency bound (barriers, plane loads). On GB300 at 512^3 the
+// the march is latency bound (barriers, plane loads). On GB300 at 512^3, with
+// the ring then filled by per-thread 16-byte cp.async copies, the plain float
 // stage time per step measured 5.30 / 5.48 / 4.80 / 4.61 / 4.48 / 4.75 ms for
 // 2 / 3 / 4 / 5 / 6 / 8 CTAs of 32 x 8 threads per SM, and 4.44 ms for twelve
 // CTAs of 32 x 4 (half the threads per barrier, 20 % more halo rows). FP64:
