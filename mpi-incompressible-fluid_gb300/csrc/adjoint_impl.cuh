@@ -25,24 +25,11 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace mifgpu {
 
 namespace adj {
-
-template <typename T>
-__device__ __forceinline__ void cp_async_elem_adj(T *smem, const T *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  if constexpr (sizeof(T) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
-}
-__device__ __forceinline__ void cp_commit_adj() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_wait_adj() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
 
 __device__ __forceinline__ bool interior(const Geometry &g, int c, int i, int j, int k) {
   return i >= 1 && j >= 1 && k >= 1 && i < g.ext(c, 0) - 1 && j < g.ext(c, 1) - 1 && k < g.ext(c, 2) - 1;
@@ -79,19 +66,31 @@ __device__ __forceinline__ T trap_weight(const Geometry &g, int i, int j, int k)
 // (Avg_{d,c} at P = Q + e_d, and the cross terms at P = Q - e_f). mu is zero
 // off the interior of its component in memory (the split kernel writes those
 // zeros and the padding is cleared once), so no read needs a mask.
-constexpr int kATX = 32, kATY = 8, kAH = 2;
-constexpr int kAHX = kATX + 2 * kAH, kAHY = kATY + 2 * kAH, kAPL = kAHX * kAHY;
+// A plane tile is one TMA box of kAHX x kAHY elements from (i0 - kAXO,
+// j0 - kAH): four columns before the tile in x, so the box starts 16-byte
+// aligned (i0 is a multiple of 32), two rows before it in y; boxes outside
+// the field read zeros. A slot is 1920 bytes in float (3840 in double), so
+// every slot starts 128-byte aligned.
+constexpr int kATX = 32, kATY = 8, kAH = 2, kAXO = 4;
+constexpr int kAHX = kATX + 2 * kAXO, kAHY = kATY + 2 * kAH, kAPL = kAHX * kAHY;
 constexpr int kASlots = 6;
+static_assert((kAPL * 4) % 128 == 0, "128-byte aligned ring slots");
 
 template <typename T>
 struct AdjRing {
   T f[6][kASlots][kAPL];  // mu_u, mu_v, mu_w, V_u, V_v, V_w; slot (k mod 6); tile
+  uint64_t bar[kASlots];  // one TMA barrier per slot
+};
+
+// Tensor maps of mu_u, mu_v, mu_w, V_u, V_v, V_w.
+struct AdjMaps {
+  CUtensorMap m[6];
 };
 
 template <typename T>
 struct ATap {
   const AdjRing<T> *r;
-  int base;      // (ty + kAH) * kAHX + tx + kAH
+  int base;      // (ty + kAH) * kAHX + tx + kAXO
   int slot[5];   // slot of plane k + dk for dk = -2 .. 2
   __device__ __forceinline__ T mu(int c, int di, int dj, int dk) const {
     return r->f[c][slot[dk + 2]][base + dj * kAHX + di];
@@ -163,44 +162,58 @@ __device__ __forceinline__ T rhs_adjoint_tap(const ATap<T> &A, const Coeffs<T> &
 }
 
 // lam_c += (R'(V)^T mu)_c on every point of the three fields.
+// The ring is filled by TMA: thread 0 loads a plane's six tiles into its slot
+// on the slot's mbarrier, and every thread waits on the barrier before
+// reading the plane (plane kk is the ((kk - kfirst) / 6)-th load of its
+// slot). A wait that gives up sets *kerr and the thread skips its later
+// waits, so the CTA still reaches every barrier and ends.
 template <typename T>
-__global__ void __launch_bounds__(kATX *kATY) rhs_adjoint_tiled(Geometry g, Coeffs<T> co, const T *m0, const T *m1,
-                                                                const T *m2, const T *v0, const T *v1, const T *v2,
-                                                                T *l0, T *l1, T *l2, int kc) {
+__global__ void __launch_bounds__(kATX *kATY) rhs_adjoint_tiled(Geometry g, Coeffs<T> co, T *l0, T *l1, T *l2,
+                                                                int kc, const __grid_constant__ AdjMaps maps,
+                                                                int *kerr) {
   extern __shared__ __align__(16) unsigned char adj_smem[];
-  AdjRing<T> &ring = *reinterpret_cast<AdjRing<T> *>(adj_smem);
-  const T *src[6] = {m0, m1, m2, v0, v1, v2};
+  AdjRing<T> &ring =
+      *reinterpret_cast<AdjRing<T> *>(adj_smem + ((128 - (smem_u32(adj_smem) & 127)) & 127));
   const int tx = threadIdx.x % kATX, ty = threadIdx.x / kATX;
   const int i0 = blockIdx.x * kATX, j0 = blockIdx.y * kATY;
   const int kbeg = blockIdx.z * kc, kend = min(kbeg + kc, g.Es[2]);
-  auto load_plane = [&](int kk) {
-    const int sl = (kk + 2 * kASlots) % kASlots;
-    for (int e = threadIdx.x; e < kAPL; e += kATX * kATY) {
-      const int hx = e % kAHX, hy = e / kAHX;
-      const int i = i0 - kAH + hx, j = j0 - kAH + hy;
-      const bool ok = kk >= 0 && kk < g.PZ && i >= 0 && i < g.PX && j >= 0 && j < g.PY;
-      const long q = ok ? g.idx(i, j, kk) : 0;
+  const int kfirst = kbeg - 2;
+  if (threadIdx.x == 0) {
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        T *d = &ring.f[f][sl][e];
-        if (ok)
-          cp_async_elem_adj(d, src[f] + q);
-        else
-          *d = T(0);
-      }
-    }
-    cp_commit_adj();
+    for (int b = 0; b < kASlots; ++b) mbar_init(&ring.bar[b], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto slot_of = [](int kk) { return (kk + 2 * kASlots) % kASlots; };
+  auto load_plane = [&](int kk) {  // thread 0
+    const int sl = slot_of(kk);
+    mbar_expect_tx(&ring.bar[sl], (unsigned)(6 * kAPL * sizeof(T)));
+#pragma unroll
+    for (int f = 0; f < 6; ++f) tma_load_3d(&ring.f[f][sl][0], &maps.m[f], i0 - kAXO, j0 - kAH, kk, &ring.bar[sl]);
   };
-  for (int kk = kbeg - 2; kk <= kbeg + 2; ++kk) load_plane(kk);
+  bool tma_ok = true;
+  auto wait_plane = [&](int kk) {
+    if (tma_ok && !mbar_wait(&ring.bar[slot_of(kk)], ((kk - kfirst) / kASlots) & 1)) {
+      tma_ok = false;
+      if (kerr) atomicExch(kerr, 1);
+    }
+  };
+  if (threadIdx.x == 0)
+    for (int kk = kbeg - 2; kk <= kbeg + 2; ++kk) load_plane(kk);
+  for (int kk = kbeg - 2; kk <= kbeg + 1; ++kk) wait_plane(kk);
   const int i = i0 + tx, j = j0 + ty;
   T *lam[3] = {l0, l1, l2};
   ATap<T> A;
   A.r = &ring;
-  A.base = (ty + kAH) * kAHX + tx + kAH;
+  A.base = (ty + kAH) * kAHX + tx + kAXO;
   for (int k = kbeg; k < kend; ++k) {
-    load_plane(k + 3);
-    cp_wait_adj<1>();
-    __syncthreads();
+    // plane k + 3 (needed while k + 3 <= kend + 1) into the slot of plane
+    // k - 3, which the barrier that ended the previous iteration released
+    if (threadIdx.x == 0 && k + 3 <= kend + 1) {
+      fence_async_shared();
+      load_plane(k + 3);
+    }
+    wait_plane(k + 2);
 #pragma unroll
     for (int dk = -2; dk <= 2; ++dk) A.slot[dk + 2] = (k + dk + 2 * kASlots) % kASlots;
     const long q = g.idx(i, j, k);
@@ -209,7 +222,6 @@ __global__ void __launch_bounds__(kATX *kATY) rhs_adjoint_tiled(Geometry g, Coef
     if (i < g.ext(2, 0) && j < g.ext(2, 1) && k < g.ext(2, 2)) lam[2][q] += rhs_adjoint_tap<T, 2>(A, co);
     __syncthreads();  // the next iteration refills the slot of plane k - 2
   }
-  cp_wait_adj<0>();
 }
 
 // out(r) = (add(r) + scale (G^T mu)(r)) / (weighted ? W(r) : 1) on the pressure
@@ -456,22 +468,31 @@ struct AdjointOps {
     }
     return co;
   }
+  // the ring and 128 bytes to align it
+  static constexpr size_t kRingSmem = sizeof(adj::AdjRing<T>) + 128;
   // Kernel attributes; call once before the first launch (outside stream capture).
   static cudaError_t prepare() {
     return cudaFuncSetAttribute(adj::rhs_adjoint_tiled<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(adj::AdjRing<T>));
+                                (int)kRingSmem);
   }
-  // Needs mu zero off each component's interior, padding included, and prepare().
-  static void rhs_adjoint(const Geometry &g, T *const lam[3], const T *const mu[3], const T *const V[3],
-                          cudaStream_t s, long long *cnt) {
+  // Needs mu zero off each component's interior, padding included, and
+  // prepare(). False (nothing launched) if a tensor map was rejected; `kerr`
+  // (device, may be null) as for the stage kernels.
+  static bool rhs_adjoint(const Geometry &g, T *const lam[3], const T *const mu[3], const T *const V[3],
+                          cudaStream_t s, long long *cnt, int *kerr = nullptr) {
     const int nx = std::max(g.Es[0], g.E[0]);
     // 8 planes per CTA below 256 planes: more, shorter CTAs; at 128^3 the
     // reverse step measured 0.734 / 0.762 / 0.777 ms for 8 / 16 / 32 (FP32).
     const int kc = g.Es[2] >= 256 ? 32 : 8;
     const dim3 grid(adj::cdiv_u(nx, adj::kATX), adj::cdiv_u(g.Es[1], adj::kATY), adj::cdiv_u(g.Es[2], kc));
-    adj::rhs_adjoint_tiled<T><<<grid, adj::kATX * adj::kATY, sizeof(adj::AdjRing<T>), s>>>(
-        g, coeffs(g), mu[0], mu[1], mu[2], V[0], V[1], V[2], lam[0], lam[1], lam[2], kc);
+    adj::AdjMaps maps;
+    const T *src[6] = {mu[0], mu[1], mu[2], V[0], V[1], V[2]};
+    for (int f = 0; f < 6; ++f)
+      if (!make_field_map(&maps.m[f], src[f], (int)sizeof(T), g.PX, g.PY, g.PZ, adj::kAHX, adj::kAHY)) return false;
+    adj::rhs_adjoint_tiled<T><<<grid, adj::kATX * adj::kATY, kRingSmem, s>>>(g, coeffs(g), lam[0], lam[1], lam[2],
+                                                                             kc, maps, kerr);
     ++*cnt;
+    return true;
   }
   static void grad_adjoint(const Geometry &g, T *out, const T *add, const T *const mu[3], double scale,
                            bool weighted, cudaStream_t s, long long *cnt) {

@@ -924,7 +924,9 @@ struct Impl final : ImplBase {
   // sets the three stage right-hand sides were evaluated at: V[0] = u_n,
   // V[1] = set 1 and V[2] = set 2 after the step. Leaves the adjoint of the
   // step's input in lx and lp and adds d loss / d alpha into *dalpha.
-  void reverse_step(mifgpu_ctx *ctx, cudaStream_t s, const T *const V[3][3], double *dalpha, long long *cnt) {
+  // False if a tensor map of the adjoint stencil was rejected (its launch
+  // and the rest of the step are then left out).
+  bool reverse_step(mifgpu_ctx *ctx, cudaStream_t s, const T *const V[3][3], double *dalpha, long long *cnt) {
     using Ops = AdjointOps<T>;
     const double dt = g.dt;
     T *lx[3] = {adj_field(kLX), adj_field(kLX + 1), adj_field(kLX + 2)};
@@ -950,8 +952,9 @@ struct Impl final : ImplBase {
       Ops::grad_adjoint(g, lp, lp, lx, -b_p[st], false, s, cnt);
       Ops::split(g, mu, pend, lx, a_own[st], st < 2 ? 1.0 : 0.0, a_prev[st], st > 0, tg ? ftab : nullptr, ftab_maxE,
                  red_part, dalpha, s, cnt);
-      Ops::rhs_adjoint(g, lx, mu, V[st], s, cnt);
+      if (!Ops::rhs_adjoint(g, lx, mu, V[st], s, cnt, nonfinite + 1)) return false;
     }
+    return true;
   }
 
   // The reverse step of snapshot slot m as a graph, captured on first use.
@@ -961,8 +964,12 @@ struct Impl final : ImplBase {
     cudaGraph_t gr = nullptr;
     CK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
     long long n = 0;
-    reverse_step(ctx, cap_stream, V, acc + 1, &n);
+    const bool maps_ok = reverse_step(ctx, cap_stream, V, acc + 1, &n);
     cudaError_t e = cudaStreamEndCapture(cap_stream, &gr);
+    if (e == cudaSuccess && !maps_ok) {
+      cudaGraphDestroy(gr);
+      return fail(ctx, MIFGPU_ECUDA, "a TMA tensor map of the adjoint stencil was rejected");
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "stream capture of the reverse step");
     e = cudaGraphInstantiate(&rev_graph[m], gr, 0);
     cudaGraphDestroy(gr);
@@ -1145,7 +1152,8 @@ struct Impl final : ImplBase {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return cleanup(), cuda_fail(ctx, e, "gradient");
-    if (flags[1]) return cleanup(), fail(ctx, MIFGPU_ECUDA, "a stage or line kernel gave up waiting for a TMA tile load");
+    if (flags[1])
+      return cleanup(), fail(ctx, MIFGPU_ECUDA, "a stage, line or adjoint kernel gave up waiting for a TMA tile load");
     if (req.loss) *req.loss = h[0];
     if (req.dalpha) *req.dalpha = h[1];
     if (req.ms) {
