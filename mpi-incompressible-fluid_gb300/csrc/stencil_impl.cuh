@@ -763,6 +763,392 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   }
 }
 
+// ---- compensated projecting stage, two points per thread ----
+//
+// stage_proj_kernel's stage with each thread owning the two x-adjacent points
+// (i, i + 1), i = i0 + 2 tx odd (i0 = 1 + 64 blockIdx.x): a CTA tile is
+// 64 x 4 points, and a row of 512 interior points is eight tiles. The two
+// points' arithmetic runs as packed two-lane float operations (add, mul and
+// fma on float2, one instruction for both points, each lane rounded as the
+// scalar operation), and the per-thread work (plane waits, masks, addresses,
+// the dither hash) is shared by the pair. The stage kernels are issue-bound,
+// so their instruction count sets their time.
+// Ring rows are 72 elements from x = i0 - 5 (a multiple of 64 minus 4: the
+// TMA box starts 16-byte aligned), so the own points sit at hx = 5 + 2 tx and
+// 6 + 2 tx: a pair of taps one point back or ahead in x starts at an even
+// index and is one 8-byte shared-memory load. The pair's global elements
+// start at an odd index, so they move as single floats.
+constexpr int kQX = 2 * kTX, kQHX = kQX + 8, kQPL = kQHX * kHY, kQSlot = 448;
+constexpr int kQPhiPL = kQHX * kPhiRows, kQPhiSlot = 512;
+static_assert(kQSlot >= kQPL && kQPhiSlot >= kQPhiPL && (kQSlot * 4) % 128 == 0 && (kQPhiSlot * 4) % 128 == 0,
+              "128-byte aligned ring slots");
+struct RingPair {
+  float f[4][4][kQSlot];  // u, v, w, p: slot (k & 3); ring point (hx, hy) at hy * kQHX + hx
+  float phi[4][kQPhiSlot];  // phi box from (i0 - 5, j0 - 2): ring point (hx, hy) at (hy + 1) * kQHX + hx
+};
+// Halo work per plane: rows hy = 0 and kTY + 1 as 32 pairs each (threads
+// 0 .. 63), columns hx = 4 and kQX + 5 for hy = 0 .. kTY + 1 as single
+// points (threads 64 .. 75).
+constexpr int kQHaloCols = 2 * (kTY + 2);
+// Resident CTAs per SM: six (36.9 KB of ring each; 80 registers a thread).
+// At 512^3 the stage class measured the same within 1 % at five CTAs.
+#ifndef MIFGPU_STAGE_PAIR_BLOCKS
+#define MIFGPU_STAGE_PAIR_BLOCKS 6
+#endif
+constexpr int kStagePairMinBlocks = MIFGPU_STAGE_PAIR_BLOCKS;
+
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b, rounded once: b * (-1) + a is exact before the rounding.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// TwoSum's error of s = fl(a + b), lane by lane.
+__device__ __forceinline__ float2 two_sum_err2(float2 a, float2 b, float2 s) {
+  const float2 bb = sub2(s, a);
+  return add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+// comp_add for a pair: hi + (lo + inc) as an error-free sum; the error in err.
+__device__ __forceinline__ float2 comp_add2(float2 hi, float2 lo, float2 inc, float2 &err) {
+  const float2 t = add2(lo, inc);
+  const float2 s = add2(hi, t);
+  err = two_sum_err2(hi, t, s);
+  return s;
+}
+// add_sr for a pair: b + c with dithers r (each in [-1/2, 1/2)) of ulp(b).
+__device__ __forceinline__ float2 add_sr2(float2 b, float2 c, float2 r) {
+  const int ea = (__float_as_int(b.x) & 0x7f800000) - (23 << 23), eb = (__float_as_int(b.y) & 0x7f800000) - (23 << 23);
+  const float2 ulp = make_float2(__int_as_float(ea > 0 ? ea : 0), __int_as_float(eb > 0 ? eb : 0));
+  return add2(b, fma2(r, ulp, c));
+}
+// Two consecutive ring elements from an even index (one 8-byte load) or from any.
+__device__ __forceinline__ float2 lda2(const float *s, int o) { return *reinterpret_cast<const float2 *>(s + o); }
+__device__ __forceinline__ float2 ldp2(const float *s, int o) { return make_float2(s[o], s[o + 1]); }
+
+// The momentum right-hand side of component c at the pair, from the ring
+// planes k - 1, k, k + 1 (m, z, p) of u, v, w at the pair's ring index o
+// (odd), include/MomentumEquation.h:42-255 term for term; also returns the
+// pair's own value (self) and p minus p one point back along c (dp).
+template <int C>
+__device__ __forceinline__ float2 rhs_pair(const float *const *U, const float *const *V, const float *const *W,
+                                           const float *const *P, int o, const Coeffs<float> &co, float2 &self,
+                                           float2 &dp) {
+  constexpr int R = kQHX;
+  float2 conv, diff;
+  if constexpr (C == 0) {
+    const float2 u13 = lda2(U[1], o - 1), u15 = lda2(U[1], o + 1), u14 = make_float2(u13.y, u15.x);
+    const float2 u11 = ldp2(U[1], o - R), u17 = ldp2(U[1], o + R), u5 = ldp2(U[0], o), u23 = ldp2(U[2], o);
+    const float2 v13 = lda2(V[1], o - 1), v14 = make_float2(v13.y, V[1][o + 1]);
+    const float2 v16 = lda2(V[1], o - 1 + R), v17 = make_float2(v16.y, V[1][o + 1 + R]);
+    const float2 w13 = lda2(W[1], o - 1), w14 = make_float2(w13.y, W[1][o + 1]);
+    const float2 w22 = lda2(W[2], o - 1), w23 = make_float2(w22.y, W[2][o + 1]);
+    const float2 p13 = lda2(P[1], o - 1), p14 = make_float2(p13.y, P[1][o + 1]);
+    const float2 a = mul2(mul2(u14, sub2(u15, u13)), splat2(co.o2h[0]));
+    const float2 b = mul2(mul2(add2(add2(add2(v17, v14), v16), v13), sub2(u17, u11)), splat2(co.o8h[1]));
+    const float2 c = mul2(mul2(add2(add2(add2(w23, w14), w22), w13), sub2(u23, u5)), splat2(co.o8h[2]));
+    conv = add2(add2(a, b), c);
+    const float2 m2 = splat2(-2.f);
+    diff = mul2(add2(fma2(u14, m2, u15), u13), splat2(co.oh2Re[0]));
+    diff = fma2(add2(fma2(u14, m2, u17), u11), splat2(co.oh2Re[1]), diff);
+    diff = fma2(add2(fma2(u14, m2, u23), u5), splat2(co.oh2Re[2]), diff);
+    self = u14;
+    dp = sub2(p14, p13);
+  } else if constexpr (C == 1) {
+    const float2 u15 = lda2(U[1], o + 1), u14 = make_float2(U[1][o], u15.x);
+    const float2 u12 = lda2(U[1], o + 1 - R), u11 = make_float2(U[1][o - R], u12.x);
+    const float2 v13 = lda2(V[1], o - 1), v15 = lda2(V[1], o + 1), v14 = make_float2(v13.y, v15.x);
+    const float2 v11 = ldp2(V[1], o - R), v17 = ldp2(V[1], o + R), v5 = ldp2(V[0], o), v23 = ldp2(V[2], o);
+    const float2 w14 = ldp2(W[1], o), w23 = ldp2(W[2], o), w11 = ldp2(W[1], o - R), w20 = ldp2(W[2], o - R);
+    const float2 p14 = ldp2(P[1], o), p11 = ldp2(P[1], o - R);
+    const float2 a = mul2(mul2(add2(add2(add2(u15, u14), u12), u11), sub2(v15, v13)), splat2(co.o8h[0]));
+    const float2 b = mul2(mul2(v14, sub2(v17, v11)), splat2(co.o2h[1]));
+    const float2 c = mul2(mul2(add2(add2(add2(w23, w14), w20), w11), sub2(v23, v5)), splat2(co.o8h[2]));
+    conv = add2(add2(a, b), c);
+    const float2 m2 = splat2(-2.f);
+    diff = mul2(add2(fma2(v14, m2, v15), v13), splat2(co.oh2Re[0]));
+    diff = fma2(add2(fma2(v14, m2, v17), v11), splat2(co.oh2Re[1]), diff);
+    diff = fma2(add2(fma2(v14, m2, v23), v5), splat2(co.oh2Re[2]), diff);
+    self = v14;
+    dp = sub2(p14, p11);
+  } else {
+    const float2 u15 = lda2(U[1], o + 1), u14 = make_float2(U[1][o], u15.x);
+    const float2 u6 = lda2(U[0], o + 1), u5 = make_float2(U[0][o], u6.x);
+    const float2 v5 = ldp2(V[0], o), v14 = ldp2(V[1], o), v17 = ldp2(V[1], o + R), v8 = ldp2(V[0], o + R);
+    const float2 w13 = lda2(W[1], o - 1), w15 = lda2(W[1], o + 1), w14 = make_float2(w13.y, w15.x);
+    const float2 w11 = ldp2(W[1], o - R), w17 = ldp2(W[1], o + R), w5 = ldp2(W[0], o), w23 = ldp2(W[2], o);
+    const float2 p14 = ldp2(P[1], o), p5 = ldp2(P[0], o);
+    const float2 a = mul2(mul2(add2(add2(add2(u15, u14), u6), u5), sub2(w15, w13)), splat2(co.o8h[0]));
+    const float2 b = mul2(mul2(add2(add2(add2(v17, v14), v8), v5), sub2(w17, w11)), splat2(co.o8h[1]));
+    const float2 c = mul2(mul2(w14, sub2(w23, w5)), splat2(co.o2h[2]));
+    conv = add2(add2(a, b), c);
+    const float2 m2 = splat2(-2.f);
+    diff = mul2(add2(fma2(w14, m2, w15), w13), splat2(co.oh2Re[0]));
+    diff = fma2(add2(fma2(w14, m2, w17), w11), splat2(co.oh2Re[1]), diff);
+    diff = fma2(add2(fma2(w14, m2, w23), w5), splat2(co.oh2Re[2]), diff);
+    self = w14;
+    dp = sub2(p14, p5);
+  }
+  return sub2(diff, conv);
+}
+
+template <int ST>
+__global__ void __launch_bounds__(kTX *kTY, kStagePairMinBlocks)
+    stage_pair_kernel(Geometry g, Coeffs<float> co, Fields<float> F, StageCoef<float> K, TimeRef tr, int kc,
+                      Residual res, StageProj pj, const __grid_constant__ StageMaps maps, int *kerr) {
+  static_assert(ST == kStageY2 || ST == kStageY3 || ST == kStageUStar, "the projection stages");
+  constexpr bool kOth = ST != kStageY2;
+  constexpr int oth_set = ST == kStageY3 ? 2 : 0;
+  __shared__ __align__(128) RingPair ring;
+  __shared__ uint64_t bars[4];
+  const long plane = g.sz(), PX = g.PX;
+  const int PZ = (int)g.PZ;
+  const int lim0 = g.ext(0, 2) - 1, lim1 = g.ext(1, 2) - 1, lim2 = g.ext(2, 2) - 1;
+  const float oh0 = co.oh[0], oh1 = co.oh[1], oh2 = co.oh[2];
+  const float2 cd0 = splat2(oh0 * pj.dt), cd1 = splat2(oh1 * pj.dt), cd2 = splat2(oh2 * pj.dt);
+  float *const p_out = pj.p_out;
+  const int tid = threadIdx.x, tx = tid % kTX, ty = tid / kTX;
+  const int i0 = 1 + blockIdx.x * kQX, j0 = 1 + blockIdx.y * kTY;
+  const int zmax = g.Es[2] - 1;  // interior k < zmax
+  const int kbeg = 1 + blockIdx.z * kc, kend = min(kbeg + kc, zmax);
+  // TMA ring fill as stage_proj_kernel's, with kQHX-wide boxes from
+  // x = i0 - 5: maps 0..3 the input set's u, v, w and p_in (rows from
+  // j0 - 1), map 4 phi (kPhiRows rows from j0 - 2).
+  const int kfirst = kbeg - 2;
+  if (tid == 0) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) mbar_init(&bars[b], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  auto load_plane = [&](int kk, bool phi_only) {  // thread 0
+    uint64_t *bar = &bars[kk & 3];
+    if (kk >= 0 && kk < PZ) {
+      mbar_expect_tx(bar, (unsigned)(sizeof(float) * (kQPhiPL + (phi_only ? 0 : 4 * kQPL))));
+      if (!phi_only)
+#pragma unroll
+        for (int f = 0; f < 4; ++f) tma_load_3d(&ring.f[f][kk & 3][0], &maps.m[f], i0 - 5, j0 - 1, kk, bar);
+      tma_load_3d(&ring.phi[kk & 3][0], &maps.m[4], i0 - 5, j0 - 2, kk, bar);
+    } else {
+      mbar_arrive(bar);
+    }
+  };
+  bool tma_ok = true;
+  auto wait_plane = [&](int kk) {
+    if (tma_ok && !mbar_wait(&bars[kk & 3], ((kk - kfirst) >> 2) & 1)) {
+      tma_ok = false;
+      if (kerr) atomicExch(kerr, 1);
+    }
+  };
+  const int i = i0 + 2 * tx, j = j0 + ty;  // the pair (i, i + 1)
+  // the other set's values at the pair and the stored residuals of the
+  // input state, prefetched one plane ahead (single elements: the pair
+  // starts at an odd index)
+  const bool in_a = i < PX && j < g.PY, in_b = i + 1 < PX && j < g.PY;
+  const long qij = (long)i + PX * (long)j;
+  const float *const oth0 = F.vel(oth_set, 0) + qij, *const oth1 = F.vel(oth_set, 1) + qij,
+                     *const oth2 = F.vel(oth_set, 2) + qij;
+  const __nv_bfloat16 *const res0 = res.c[0] + qij, *const res1 = res.c[1] + qij, *const res2 = res.c[2] + qij;
+  float2 n0 = splat2(0.f), n1 = n0, n2 = n0, l0 = n0, l1 = n0, l2 = n0;
+  auto prefetch = [&](int kk) {
+    if (kk >= kend) return;
+    const long po = (long)kk * plane;
+    if (in_a) {
+      if (kOth) n0.x = oth0[po], n1.x = oth1[po], n2.x = oth2[po];
+      l0.x = __bfloat162float(res0[po]), l1.x = __bfloat162float(res1[po]), l2.x = __bfloat162float(res2[po]);
+    }
+    if (in_b) {
+      if (kOth) n0.y = oth0[po + 1], n1.y = oth1[po + 1], n2.y = oth2[po + 1];
+      l0.y = __bfloat162float(res0[po + 1]), l1.y = __bfloat162float(res1[po + 1]),
+      l2.y = __bfloat162float(res2[po + 1]);
+    }
+  };
+  // Interior masks in x and y, bit c + 3 s for component c at point s: the
+  // own pair (s = 0, 1) and this thread's halo pair or point (s = 2, 3).
+  auto xy_mask = [&](int x, int y) {
+    unsigned m = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if (x >= 1 && y >= 1 && x < g.ext(c, 0) - 1 && y < g.ext(c, 1) - 1) m |= 1u << c;
+    return m;
+  };
+  const bool h_pair = tid < 2 * kTX, h_single = tid >= 2 * kTX && tid < 2 * kTX + kQHaloCols;
+  int h_r = 0, h_p = 0;
+  unsigned msk = xy_mask(i, j) | (xy_mask(i + 1, j) << 3);
+  {
+    int hx = 0, hy = 0;
+    if (tid < kTX) hx = 5 + 2 * tid, hy = 0;
+    else if (tid < 2 * kTX) hx = 5 + 2 * (tid - kTX), hy = kTY + 1;
+    else if (tid < 2 * kTX + kTY + 2) hx = 4, hy = tid - 2 * kTX;
+    else hx = kQX + 5, hy = tid - 2 * kTX - (kTY + 2);
+    h_r = hy * kQHX + hx;
+    h_p = (hy + 1) * kQHX + hx;
+    const int hi_ = i0 - 5 + hx, hj = j0 - 1 + hy;
+    if (h_pair) msk |= (xy_mask(hi_, hj) << 6) | (xy_mask(hi_ + 1, hj) << 9);
+    if (h_single) msk |= xy_mask(hi_, hj) << 6;
+  }
+  const int o_r = (ty + 1) * kQHX + 5 + 2 * tx, o_p = o_r + kQHX;  // own ring / phi index (odd)
+  float2 e0 = splat2(0.f), e1 = e0, e2 = e0;  // the own pair's exact residuals at the plane projected last
+  // Projection of ring plane kk (u' = fl(u + inc), inc = (phi_b - phi) oh dt,
+  // on the points interior to the component); with own_exact the own pair's
+  // stored residuals lo become lo + e (e0..e2). (Adding the stored residual
+  // one plane later instead, so that its load had a plane of work to land,
+  // kept six more registers live; the spills cost more than the wait.)
+  auto project_plane = [&](int kk, bool own_exact) {
+    float *const rb = ring.f[0][kk & 3];
+    const float *const ph = ring.phi[kk & 3], *const phb = ring.phi[(kk - 1) & 3];
+    const unsigned kin = (kk >= 1) ? ((kk < lim0 ? 1u : 0u) | (kk < lim1 ? 2u : 0u) | (kk < lim2 ? 4u : 0u)) : 0u;
+    const unsigned m = msk & (kin * 0x249u);  // kin in every point's bits
+    {
+      const float2 fm = lda2(ph, o_p - 1), fp = lda2(ph, o_p + 1), f0 = make_float2(fm.y, fp.x);
+      float2 lo[3] = {l0, l1, l2};
+      const float2 fb[3] = {fm, ldp2(ph, o_p - kQHX), ldp2(phb, o_p)};
+      const float2 cd[3] = {cd0, cd1, cd2};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const bool ma = (m >> c) & 1u, mb = (m >> (3 + c)) & 1u;
+        if (!(ma || mb)) continue;
+        float *const r = rb + c * 4 * kQSlot + o_r;
+        const float2 hi = make_float2(r[0], r[1]);
+        const float2 inc = mul2(sub2(fb[c], f0), cd[c]);
+        const float2 s = add2(hi, inc);
+        const float2 e = two_sum_err2(hi, inc, s);
+        if (ma) r[0] = s.x, lo[c].x = __fadd_rn(lo[c].x, e.x);
+        if (mb) r[1] = s.y, lo[c].y = __fadd_rn(lo[c].y, e.y);
+      }
+      if (own_exact) e0 = lo[0], e1 = lo[1], e2 = lo[2];
+    }
+    if (h_pair && (m & 0xfc0u)) {
+      const float2 fm = lda2(ph, h_p - 1), fp = lda2(ph, h_p + 1), f0 = make_float2(fm.y, fp.x);
+      const float2 fb[3] = {fm, ldp2(ph, h_p - kQHX), ldp2(phb, h_p)};
+      const float2 cd[3] = {cd0, cd1, cd2};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const bool ma = (m >> (6 + c)) & 1u, mb = (m >> (9 + c)) & 1u;
+        if (!(ma || mb)) continue;
+        float *const r = rb + c * 4 * kQSlot + h_r;
+        const float2 s = add2(make_float2(r[0], r[1]), mul2(sub2(fb[c], f0), cd[c]));
+        if (ma) r[0] = s.x;
+        if (mb) r[1] = s.y;
+      }
+    } else if (h_single && (m & 0x1c0u)) {
+      const float f0 = ph[h_p];
+      if (m & 0x40u) rb[h_r] = __fadd_rn(rb[h_r], (ph[h_p - 1] - f0) * cd0.x);
+      if (m & 0x80u) rb[4 * kQSlot + h_r] = __fadd_rn(rb[4 * kQSlot + h_r], (ph[h_p - kQHX] - f0) * cd1.x);
+      if (m & 0x100u) rb[8 * kQSlot + h_r] = __fadd_rn(rb[8 * kQSlot + h_r], (phb[h_p] - f0) * cd2.x);
+    }
+  };
+  // p + phi, stochastically rounded: the pair's two dithers from one hash.
+  const unsigned psalt = sr_salt(tr, pj.tag);
+  auto p_new1 = [&](int r, int rp, int kk, long q) {
+    return add_sr(ring.f[3][kk & 3][r], ring.phi[kk & 3][rp], sr_draw(sr_mix((unsigned)q ^ psalt), 0));
+  };
+  // Pressure nodes outside the threads' range, at the CTAs on those edges.
+  const int E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
+  const bool edge_x0 = blockIdx.x == 0, edge_y0 = blockIdx.y == 0, edge_xr = i0 + kQX == E0 - 1;
+  auto write_p_edges = [&](int kk) {
+    auto one = [&](int hx, int hy) {
+      const int pi = i0 - 5 + hx, pjj = j0 - 1 + hy;
+      if (pi >= E0 || pjj >= E1 || kk >= E2) return;
+      const long q = pi + PX * (pjj + g.PY * (long)kk);
+      p_out[q] = p_new1(hy * kQHX + hx, (hy + 1) * kQHX + hx, kk, q);
+    };
+    if (edge_x0 && tx == 0) one(4, ty + 1);
+    if (edge_xr && tx == kTX - 1) one(kQX + 5, ty + 1);
+    if (edge_y0 && ty == 0) {
+      one(5 + 2 * tx, 0);
+      one(6 + 2 * tx, 0);
+      if (edge_x0 && tx == 0) one(4, 0);
+      if (edge_xr && tx == kTX - 1) one(kQX + 5, 0);
+    }
+  };
+  const bool own_pa = i < E0 && j < E1, own_pb = i + 1 < E0 && j < E1;
+  auto write_p_pair = [&](int kk, long q) {
+    const float2 pv = ldp2(ring.f[3][kk & 3], o_r), fv = ldp2(ring.phi[kk & 3], o_p);
+    const unsigned h = sr_mix((unsigned)q ^ psalt);
+    const float2 s = add_sr2(pv, fv, make_float2(sr_draw(h, 0), sr_draw(h, 1)));
+    if (own_pa) p_out[q] = s.x;
+    if (own_pb) p_out[q + 1] = s.y;
+  };
+  const bool edges = edge_x0 | edge_y0 | edge_xr;
+  // Prologue: phi of plane kbeg - 2 (w's projection of plane kbeg - 1), the
+  // planes kbeg - 1 .. kbeg + 1; planes kbeg - 1 and kbeg projected.
+  if (tid == 0) {
+    load_plane(kbeg - 2, true);
+    load_plane(kbeg - 1, false);
+    load_plane(kbeg, false);
+    load_plane(kbeg + 1, false);
+  }
+  wait_plane(kbeg - 2);
+  wait_plane(kbeg - 1);
+  wait_plane(kbeg);
+  project_plane(kbeg - 1, false);
+  prefetch(kbeg);
+  project_plane(kbeg, true);
+  if (kbeg == 1) {  // the pressure of plane 0, which no thread's march reaches
+    write_p_pair(0, qij);
+    if (edges) write_p_edges(0);
+  }
+  __syncthreads();  // the first iteration refills the slot of plane kbeg - 2
+  for (int k = kbeg; k < kend; ++k) {
+    if (tid == 0 && k + 2 <= kend) {
+      fence_async_shared();
+      load_plane(k + 2, false);
+    }
+    const float2 c0 = n0, c1 = n1, c2 = n2, lo0 = e0, lo1 = e1, lo2 = e2;
+    prefetch(k + 1);
+    wait_plane(k + 1);
+    project_plane(k + 1, true);
+    __syncthreads();
+    const float *U[3], *V[3], *W[3], *P[3];
+#pragma unroll
+    for (int dk = -1; dk <= 1; ++dk) {
+      U[dk + 1] = ring.f[0][(k + dk) & 3];
+      V[dk + 1] = ring.f[1][(k + dk) & 3];
+      W[dk + 1] = ring.f[2][(k + dk) & 3];
+      P[dk + 1] = ring.f[3][(k + dk) & 3];
+    }
+    const float *const ph = ring.phi[k & 3], *const phb = ring.phi[(k - 1) & 3];
+    const float2 fm = lda2(ph, o_p - 1), fp = lda2(ph, o_p + 1), f14 = make_float2(fm.y, fp.x);
+    const long q = qij + (long)k * plane;
+    auto update = [&](auto cc, const float2 &cur, const float2 &lo, float2 fb, float ohc) {
+      constexpr int c = decltype(cc)::value;
+      const bool ma = (msk >> c) & 1u, mb = (msk >> (3 + c)) & 1u;
+      if (!(ma || mb) || k >= (c == 0 ? lim0 : (c == 1 ? lim1 : lim2))) return;
+      float2 self, dp;
+      const float2 r = rhs_pair<c>(U, V, W, P, o_r, co, self, dp);
+      const float2 gp = mul2(add2(dp, sub2(f14, fb)), splat2(ohc));
+      float2 inc, err, s;
+      float *const out_s = F.vel(ST == kStageY2 ? 1 : (ST == kStageY3 ? 2 : 0), c) + q;
+      if constexpr (ST == kStageY2) {
+        inc = fma2(splat2(-K.k3), gp, mul2(splat2(K.k1), r));
+      } else if constexpr (ST == kStageY3) {
+        const float2 r2s = mul2(splat2(K.k2), r);
+        inc = fma2(splat2(-K.k3), gp, fma2(splat2(K.k1), cur, r2s));
+        float *const out_r = F.vel(0, c) + q;
+        if (ma) out_r[0] = r2s.x;
+        if (mb) out_r[1] = r2s.y;
+      } else {
+        inc = sub2(fma2(splat2(-K.k3), gp, mul2(splat2(K.k2), r)), cur);
+      }
+      s = comp_add2(self, lo, inc, err);
+      __nv_bfloat16 *const lo_out = res.c[c] + q;
+      if (ma) out_s[0] = s.x, lo_out[0] = __float2bfloat16_rn(err.x);
+      if (mb) out_s[1] = s.y, lo_out[1] = __float2bfloat16_rn(err.y);
+      if constexpr (ST == kStageY2) {
+        float *const out_r = F.vel(2, c) + q;
+        if (ma) out_r[0] = r.x;
+        if (mb) out_r[1] = r.y;
+      }
+    };
+    update(std::integral_constant<int, 0>{}, c0, lo0, fm, oh0);
+    update(std::integral_constant<int, 1>{}, c1, lo1, ldp2(ph, o_p - kQHX), oh1);
+    update(std::integral_constant<int, 2>{}, c2, lo2, ldp2(phb, o_p), oh2);
+    write_p_pair(k, q);
+    if (edges) write_p_edges(k);
+    __syncthreads();  // the next iteration refills the slot of plane k - 1
+  }
+}
+
 // ---- boundary fill, src/VelocityTensor.cpp:36-233 ----
 
 // Sampling point of component c at index (i,j,k): staggered (face) along c.
@@ -1474,13 +1860,16 @@ struct StageLaunch {
   int *kerr;
   // The tensor maps of the ring fields: the input set's u, v, w and p (the
   // projecting stages' p_in), and phi for the projecting stages.
-  bool maps_for(int in_set, bool with_phi, StageMaps &m) const {
+  // Box widths: kHX (phi kPhiX) for the one-point-per-thread kernels, kQHX
+  // for both in the pair kernel.
+  bool maps_for(int in_set, bool with_phi, StageMaps &m, bool pair = false) const {
     const T *src[4] = {F.vel(in_set, 0), F.vel(in_set, 1), F.vel(in_set, 2), F.f[kP]};
     if (proj) src[3] = reinterpret_cast<const T *>(proj->p_in);
+    const int bx = pair ? kQHX : kHX, pbx = pair ? kQHX : kPhiX;
     for (int f = 0; f < 4; ++f)
-      if (!make_field_map(&m.m[f], src[f], (int)sizeof(T), g.PX, g.PY, g.PZ, kHX, kHY)) return false;
+      if (!make_field_map(&m.m[f], src[f], (int)sizeof(T), g.PX, g.PY, g.PZ, bx, kHY)) return false;
     m.m[4] = m.m[3];
-    return !with_phi || make_field_map(&m.m[4], proj->phi, (int)sizeof(float), g.PX, g.PY, g.PZ, kPhiX, kPhiRows);
+    return !with_phi || make_field_map(&m.m[4], proj->phi, (int)sizeof(float), g.PX, g.PY, g.PZ, pbx, kPhiRows);
   }
   template <int ST>
   bool go(bool comp) const {
@@ -1489,6 +1878,14 @@ struct StageLaunch {
                                                                                : 2;
     StageMaps m;
     if constexpr (std::is_same<T, float>::value && ST <= kStageUStar) {
+      if (comp && proj && !forcing) {
+        // two points per thread: 64-point tiles in x
+        if (!maps_for(in_set, true, m, true)) return false;
+        const int ni = g.Es[0] > g.E[0] ? g.Es[0] : g.E[0];
+        const dim3 pgrid(cdiv(ni - 2, kQX), grid.y, grid.z);
+        stage_pair_kernel<ST><<<pgrid, blk, 0, s>>>(g, co, F, K, tr, kc, res, *proj, m, kerr);
+        return true;
+      }
       if (comp && proj) {
         if (!maps_for(in_set, true, m)) return false;
         if (forcing)
