@@ -39,6 +39,18 @@ namespace mifgpu {
 namespace {
 
 constexpr int kThreads = 256;
+// Threads of a register-path CTA (its line pairs: this over the FFT shape's
+// second factor). The kernels take their thread count from the launch, up
+// to kThreads. A CTA loads all its lines before its FFTs start, so its load
+// and compute overlap only with other CTAs': at 128 threads six CTAs share an
+// SM (the same 24 warps as three of 256). At 512^3 (32 x 16 shapes) the x, y
+// and fused z sweeps took 0.89, 0.93 and 1.72 ms per step with 256 threads,
+// 0.81, 0.85 and 1.66 with 128, 0.83, 0.91 and 1.86 with 64.
+#ifndef MIFGPU_REG_THREADS
+#define MIFGPU_REG_THREADS 128
+#endif
+constexpr int kRegThreads = MIFGPU_REG_THREADS;
+static_assert(kRegThreads <= kThreads && (kRegThreads & (kRegThreads - 1)) == 0, "register-path CTA size");
 
 template <typename T>
 struct MaxE;
@@ -556,10 +568,11 @@ __device__ __forceinline__ void reg_fft_core(typename Vec2<T>::type (&x)[N1], ty
   }
 }
 
-// Three CTAs per SM (at most 80 registers; the rows of the 32 x 16 shape
-// allow three). The fused z sweep spills ~200 bytes at that bound but still
-// ran 2.5% faster on GB300 than at two CTAs (128 registers). The 48-point
-// shapes keep two (96 registers of data; their rows allow two CTAs anyway).
+// The register budget of three kThreads-thread CTAs per SM (at most 80
+// registers; with kRegThreads = 128, six CTAs of half the size). The fused
+// z sweep spills ~200 bytes at that bound but still ran 2.5% faster on GB300
+// than with 128 registers. The 48-point shapes keep the budget of two (96
+// registers of data; their rows allow no more CTAs anyway).
 template <int N1, int MODE>
 struct RegMinBlocks {
   static constexpr int v = N1 >= 48 ? 2 : 3;
@@ -674,7 +687,7 @@ __global__ void __launch_bounds__(kThreads, RegMinBlocks<N1, MODE>::v)
     const char *e0 = reinterpret_cast<const char *>(a.eig + table.eoff[0] * n);
     const char *e1 = reinterpret_cast<const char *>(a.eig + (table.eoff[last - line0] + 1) * n);
     if (table.eoff[last - line0] == table.eoff[0] + (last - line0))
-      for (const char *q = e0 + 128 * threadIdx.x; q < e1; q += 128 * kThreads)
+      for (const char *q = e0 + 128 * threadIdx.x; q < e1; q += 128 * blockDim.x)
         asm volatile("prefetch.global.L2 [%0];\n" ::"l"(q));
   }
   if (tma) {
@@ -848,7 +861,7 @@ static void launch_reg(int n1, int n2, int mode, unsigned grid, size_t smem, cud
   const void *fn = RegKernels<T>::get(n1, n2, mode, a.kind);
   CUtensorMap map = tmap;
   void *args[] = {&a, &map};
-  cudaLaunchKernel(fn, dim3(grid), dim3(kThreads), args, smem, stream);
+  cudaLaunchKernel(fn, dim3(grid), dim3(a.P * (unsigned)n2), args, smem, stream);
 }
 
 
@@ -919,7 +932,7 @@ int AxisPlan<T>::build(int kind_, int n_, double h, int line_count, bool line_fa
       reg_n1 = 48;  // 3 x 2^k: 48 x 8 or 48 x 16
     }
     reg_n2 = reg_L / reg_n1;
-    reg_P = kThreads / reg_n2;
+    reg_P = kRegThreads / reg_n2;
     reg_lg = 0;
     while ((1 << reg_lg) < 2 * reg_P) ++reg_lg;
     reg_smem = sizeof(typename Vec2<T>::type) * (size_t)reg_P * (size_t)(reg_n1 * (reg_n2 + 1) + 2);  // RegShape::ROW
