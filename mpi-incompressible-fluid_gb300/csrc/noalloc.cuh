@@ -7,8 +7,9 @@
 
 namespace mifgpu {
 
-// Interior z planes the static scratch has room for: 3 partial sums per plane
-// plus the 3 results, (4000 + 1) * 3 doubles = 96 KB.
+// Partial-sum slots of the static scratch: 3 partial sums per slot plus the
+// 3 results, (4000 + 1) * 3 doubles = 96 KB. Each interior z plane takes at
+// least one slot, so this is also the largest number of interior planes.
 constexpr int kNoAllocMaxPlanes = 4000;
 
 // Device address of the scratch on the current device, looked up with
@@ -17,9 +18,12 @@ constexpr int kNoAllocMaxPlanes = 4000;
 int noalloc_scratch(double **out, std::string &err);
 
 // Two-pass reduction of src/Norms.cpp:11-47 over velocity set (u, v, w):
-// one block per interior z plane writes that plane's (sum |e|, sum e^2,
-// max |e|) to scratch[3 k], then one block adds the planes in index order and
-// writes the three totals to scratch[3 kNoAllocMaxPlanes]. Every scratch
+// each interior z plane is split into the same number of chunks (as many as
+// the slots allow, each of at least 1024 points, so that flat grids fill the
+// GPU too); one block per chunk writes its (sum |e|, sum e^2, max |e|) to its
+// own slot, then one block adds the slots in index order and writes the three
+// totals to scratch[3 kNoAllocMaxPlanes]. The split depends on the grid only,
+// so the result is the same on every call. Every scratch
 // element read is written earlier in the same call, so nothing has to start
 // at zero. Needs E[2] - 2 <= kNoAllocMaxPlanes (the caller checks). With `res`
 // on, the velocity is hi + residual (the compensated state).

@@ -3,6 +3,7 @@
 // instead of memory the context allocates. The per-point arithmetic is that
 // of velocity_error_kernel (src/Norms.cpp:11-47): velocity averaged to the
 // interior nodes, compared with the analytic family in double.
+#include <algorithm>
 #include <mutex>
 
 #include "analytic.cuh"
@@ -15,7 +16,8 @@ namespace {
 constexpr int kNT = 256;
 constexpr int kMaxDevices = 64;
 
-// [3 * k .. 3 * k + 2]: plane k's (sum |e|, sum e^2, max |e|);
+// [3 * k .. 3 * k + 2]: slot k's (sum |e|, sum e^2, max |e|), one slot per
+// (interior plane, chunk);
 // [3 * kNoAllocMaxPlanes .. + 2]: the totals.
 static __device__ __align__(256) double g_norm_scratch[3 * (kNoAllocMaxPlanes + 1)];
 
@@ -44,14 +46,19 @@ __device__ void block_sum2_max(double &a, double &b, double &m) {
   }
 }
 
-template <typename T>
+// Block b takes chunk b % chunks of interior plane 1 + b / chunks: the
+// points [c len, (c + 1) len) of the plane's ni x nj interior, x fastest.
+// I: the index type of a plane's points (32-bit where the plane fits).
+template <typename T, typename I>
 __global__ void __launch_bounds__(kNT) velocity_error_plane_kernel(Geometry g, const T *u, const T *v, const T *w,
-                                                                   int kind, double t, double *part, Residual res) {
-  const long ni = g.E[0] - 2, nj = g.E[1] - 2;
-  const long k = 1 + blockIdx.x;
+                                                                   int kind, double t, int chunks, I len,
+                                                                   double *part, Residual res) {
+  const I ni = (I)(g.E[0] - 2), n = ni * (I)(g.E[1] - 2);
+  const long k = 1 + blockIdx.x / chunks;
+  const I c = (I)(blockIdx.x % chunks), end = n < (c + 1) * len ? n : (c + 1) * len;
   double a = 0, b = 0, m = 0;
-  for (long id = threadIdx.x; id < ni * nj; id += kNT) {
-    const long i = 1 + id % ni, j = 1 + id / ni;
+  for (I id = c * len + threadIdx.x; id < end; id += kNT) {
+    const long i = 1 + (long)(id % ni), j = 1 + (long)(id / ni);
     const long q = g.idx(i, j, k);
     const double x = g.origin[0] + (double)(g.base[0] + i) * g.h[0];
     const double y = g.origin[1] + (double)(g.base[1] + j) * g.h[1];
@@ -78,9 +85,9 @@ __global__ void __launch_bounds__(kNT) velocity_error_plane_kernel(Geometry g, c
   }
 }
 
-__global__ void __launch_bounds__(kNT) plane_totals_kernel(const double *part, int planes, double *out) {
+__global__ void __launch_bounds__(kNT) plane_totals_kernel(const double *part, int slots, double *out) {
   double a = 0, b = 0, m = 0;
-  for (int k = threadIdx.x; k < planes; k += kNT) {
+  for (int k = threadIdx.x; k < slots; k += kNT) {
     a += part[3 * k + 0];
     b += part[3 * k + 1];
     m = fmax(m, part[3 * k + 2]);
@@ -152,8 +159,17 @@ template <typename T>
 void launch_velocity_errors_noalloc(const Geometry &g, const T *u, const T *v, const T *w, int field_kind, double t,
                                     double *scratch, cudaStream_t s, long long *launches, const Residual &res) {
   const int planes = g.E[2] - 2;
-  velocity_error_plane_kernel<T><<<planes, kNT, 0, s>>>(g, u, v, w, field_kind, t, scratch, res);
-  plane_totals_kernel<<<1, kNT, 0, s>>>(scratch, planes, scratch + 3 * kNoAllocMaxPlanes);
+  const long n = (long)(g.E[0] - 2) * (g.E[1] - 2);
+  const long by_points = std::max(1L, n / 1024);
+  const int chunks = (int)std::max(1L, std::min((long)(kNoAllocMaxPlanes / std::max(planes, 1)), by_points));
+  const long len = (n + chunks - 1) / chunks;
+  const unsigned blocks = (unsigned)(planes * chunks);
+  if (n + len + kNT < (1L << 31))  // every index the chunk loop forms fits an int
+    velocity_error_plane_kernel<T, int>
+        <<<blocks, kNT, 0, s>>>(g, u, v, w, field_kind, t, chunks, (int)len, scratch, res);
+  else
+    velocity_error_plane_kernel<T, long><<<blocks, kNT, 0, s>>>(g, u, v, w, field_kind, t, chunks, len, scratch, res);
+  plane_totals_kernel<<<1, kNT, 0, s>>>(scratch, planes * chunks, scratch + 3 * kNoAllocMaxPlanes);
   if (launches) *launches += 2;
 }
 

@@ -40,6 +40,26 @@ def test_noalloc_norms_match_error_norms(mifgpu_lib, cuda_device, precision, per
     s.close()
 
 
+@pytest.mark.parametrize("precision", [0, 2], ids=["fp64", "compensated"])
+def test_noalloc_norms_split_flat_planes(mifgpu_lib, cuda_device, precision):
+    """A flat grid (three interior planes of 127 x 128 points): each plane is
+    split into 15 chunks, the last one short, and the result still matches
+    error_norms and repeats bit for bit."""
+    mg = mifgpu_lib
+    s = make(mg, (129, 130, 5), precision, kind=1)
+    s.set_exact_velocity(0, 0.3)
+    rng = np.random.default_rng(5)
+    for name in ("u", "v", "w"):
+        f = s.download(name)
+        s.upload(name, f + 1e-3 * rng.standard_normal(f.shape))
+    want = s.error_norms(0.3)[:3]
+    first = s.velocity_error_norms_noalloc(0.3)
+    second = s.velocity_error_norms_noalloc(0.3)
+    np.testing.assert_array_equal(first, second)
+    np.testing.assert_allclose(first, want, rtol=1e-12, atol=0)
+    s.close()
+
+
 def test_noalloc_norms_reject_too_many_planes(mifgpu_lib, cuda_device):
     """A z extent of 4098 points (4096 interior planes) exceeds the 4000-plane scratch."""
     mg = mifgpu_lib
