@@ -678,7 +678,10 @@ __global__ void __launch_bounds__(kTX *kTY, kStageProjMinBlocks)
   };
   // Pressure nodes outside the threads' range, at the CTAs on those edges.
   const int E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
-  const bool edge_x0 = blockIdx.x == 0, edge_y0 = blockIdx.y == 0, edge_xr = i0 + kTX == E0 - 1;
+  // the last node E0 - 1 is the right halo only of the last tile (else a
+  // later tile owns it)
+  const bool edge_x0 = blockIdx.x == 0, edge_y0 = blockIdx.y == 0,
+             edge_xr = i0 + kTX == E0 - 1 && blockIdx.x + 1 == gridDim.x;
   auto write_p_edges = [&](int kk) {
     auto one = [&](int hx, int hy) {
       const int pi = i0 - 1 + hx, pjj = j0 - 1 + hy;
@@ -1044,7 +1047,10 @@ __global__ void __launch_bounds__(kTX *kTY, kStagePairMinBlocks)
   };
   // Pressure nodes outside the threads' range, at the CTAs on those edges.
   const int E0 = g.E[0], E1 = g.E[1], E2 = g.E[2];
-  const bool edge_x0 = blockIdx.x == 0, edge_y0 = blockIdx.y == 0, edge_xr = i0 + kQX == E0 - 1;
+  // the last node E0 - 1 is the right halo only of the last tile (else a
+  // later tile owns it)
+  const bool edge_x0 = blockIdx.x == 0, edge_y0 = blockIdx.y == 0,
+             edge_xr = i0 + kQX == E0 - 1 && blockIdx.x + 1 == gridDim.x;
   auto write_p_edges = [&](int kk) {
     auto one = [&](int hx, int hy) {
       const int pi = i0 - 5 + hx, pjj = j0 - 1 + hy;
