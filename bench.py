@@ -110,7 +110,7 @@ def sweeps(precision: str) -> dict:
         for k, v in COMPENSATED_EXTRA.items():
             out[k] += v
         # The stage kernels of the step a run repeats (the one profile_step
-        # times) apply the projection before them (stage_proj_kernel): each
+        # times) apply the projection before them (stage_pair_kernel): each
         # also reads phi and writes p + phi (15, 18, 15).
         out["stage"] += 2.0
     return out
