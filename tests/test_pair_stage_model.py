@@ -108,6 +108,11 @@ def cta_writes(g, bx, by):
 
 
 GEOMETRIES = [
+    # the smallest grids the library accepts
+    ((3, 3, 3), (False, False, False)),
+    ((4, 3, 5), (True, False, True)),
+    ((3, 4, 3), (True, True, True)),
+    ((5, 3, 4), (False, True, False)),
     ((9, 9, 9), (False, False, False)),
     ((17, 18, 19), (False, False, False)),
     ((26, 27, 28), (False, True, False)),
