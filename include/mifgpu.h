@@ -31,7 +31,10 @@ extern "C" {
 
 #define MIFGPU_OK 0
 #define MIFGPU_EINVAL (-1)   /* bad argument (null pointer, size, id, mode) */
-#define MIFGPU_ECUDA (-2)    /* a CUDA call failed; see mifgpu_last_error */
+#define MIFGPU_ECUDA (-2)    /* a CUDA call failed, a TMA tensor map was
+                                rejected, or a kernel gave up waiting for a
+                                TMA tile load (each wait is bounded); see
+                                mifgpu_last_error */
 #define MIFGPU_ENOMEM (-3)   /* device allocation failed */
 #define MIFGPU_ENOTSUP (-4)  /* combination the reference does not define */
 #define MIFGPU_ENONFINITE (-5) /* a projection step produced NaN/Inf: the last
